@@ -1,0 +1,420 @@
+"""Benchmark: sparse-voxel-DAG ray traversal throughput on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload terrain-4096|spheres-256] [--kernel plain|persistent]
+
+Workload (default terrain-4096): the seeded 4096^3 terrain DAG; one step traces
+4,194,304 primary rays (2048x2048 pinhole) and 4,194,304 cosine-weighted bounce
+rays from the primary hits, i.e. two traversal launches over 8,388,608 rays.
+Inputs are resident in HBM before timing; the ray and hit arrays (654 MB per
+step) exceed the 129 MB L2, so each step streams them; the 115 MB DAG is the
+traversal's working set and stays in L2.
+
+`value` is device throughput (CUDA events on the launching stream); `e2e` is the
+same workload through the host-buffer C ABI (cbq_intersect_host) with pinned
+host rays in and hits out, copies inside the timed region.
+
+Multi-GPU (torchrun, N > 1): replicas only.  Rays are independent and the DAG is
+read-only, so every rank traces its own full replica; there is no data-path
+collective, only the timing barrier and a max-over-ranks of the elapsed time.
+
+--impl reference times the reference's CPU ray cast on the host cores on the
+same workload: the reference's own library (oracle/_ref, where it could be
+compiled from the reference checkout) or else the oracle's C restatement of it.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+HIT_BYTES = 1 + 4 + 4 + 12 + 12 + 12 + 1  # hit, distance, material, position, normal, voxel, status
+RAY_BYTES = 32
+SECTOR = 32
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--workload", choices=["terrain-4096", "spheres-256"], default="terrain-4096")
+    p.add_argument("--kernel", choices=["plain", "persistent"], default="plain")
+    p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+# ------------------------------------------------------------------ workload
+
+def make_workload(name: str):
+    """Returns (nodes, root, [(label, origin_tmax, direction), ...])."""
+    import cubiquity_gb300 as cbq
+    from cubiquity_gb300 import workloads as W
+
+    if name == "spheres-256":
+        nodes, root = W.SPHERES_256.build()
+        o, d = W.SPHERES_256_CAMERA.rays()
+        return nodes, root, [("primary", o, d)], None
+    nodes, root = W.TERRAIN_4096.build()
+    o, d = W.TERRAIN_4096_CAMERA.rays()
+    return nodes, root, [("primary", o, d)], "bounce"
+
+
+def bounce_batch(dag, o, d):
+    """Bounce rays from the primary hits (traced once on the GPU during set-up)."""
+    import torch
+    import cubiquity_gb300 as cbq
+    from cubiquity_gb300 import workloads as W
+
+    out = cbq.intersect_volume(dag, torch.from_numpy(o).cuda(), torch.from_numpy(d).cuda())
+    torch.cuda.synchronize()
+    bo, bd = W.bounce_from_hits(out, o.shape[0])
+    return bo, bd
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = max(smax, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ helpers
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            j = json.loads(p.read_text())
+            return float(j["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(workload: str):
+    """DRAM bytes per launch from the committed ncu summary, if one exists."""
+    f = ROOT / "profiles" / f"traverse_{workload}.md"
+    if not f.exists():
+        return None
+    m = re.search(r"dram_bytes_per_ray:\s*([0-9.]+)", f.read_text())
+    return float(m.group(1)) if m else None
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "gb300" else "gloo"
+        if args.impl == "gb300":
+            import torch
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, value: float) -> float:
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ CPU arms
+
+def cpu_trace(nodes, root, batches, threads=0):
+    """Times the reference CPU ray cast over the batches; returns (seconds, kind)."""
+    import oracle
+
+    if oracle.reference_available():
+        ref = oracle.Reference()
+        vol = ref.volume_from_nodes(nodes, root)
+        sd = vol.find_subdags()
+        t0 = time.perf_counter()
+        for _, o, d in batches:
+            vol.intersect(sd, o, d, True, -1.0, threads)
+        return time.perf_counter() - t0, "reference"
+    orc = oracle.Oracle()
+    sd = orc.find_subdags(nodes, root)
+    t0 = time.perf_counter()
+    for _, o, d in batches:
+        orc.intersect(nodes, sd, o, d, True, -1.0, threads=threads)
+    return time.perf_counter() - t0, "port"
+
+
+def host_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    nodes, root, batches, bounce = make_workload(args.workload)
+    if bounce:
+        import oracle
+        orc = oracle.Oracle()
+        prim = orc.intersect(nodes, orc.find_subdags(nodes, root), batches[0][1], batches[0][2])
+        from cubiquity_gb300 import workloads as W
+        bo, bd = W.bounce_from_hits(prim, batches[0][1].shape[0])
+        batches.append(("bounce", bo, bd))
+    rays = sum(b[1].shape[0] for b in batches)
+    for _ in range(args.warmup):
+        cpu_trace(nodes, root, batches)
+    total = 0.0
+    kind = "port"
+    for _ in range(args.steps):
+        dt, kind = cpu_trace(nodes, root, batches)
+        total += dt
+    value = rays * args.steps / total / 1e6
+    cores = host_cores()
+    line = {
+        "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene, generated rays)",
+        "impl": "reference",
+        "config": {"workload": args.workload, "rays_per_step": rays},
+        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": cores, "kind": kind,
+                         "sample": f"full workload ({rays} rays) per step, intersectVolume with "
+                                   f"computeSurfaceProperties=true on {cores} host threads"},
+        "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def run_gpu(args, world, rank, local):
+    import torch
+    import cubiquity_gb300 as cbq
+
+    torch.cuda.set_device(local)
+    nodes, root, batches, bounce = make_workload(args.workload)
+    dag = cbq.Dag(nodes, root)
+    if bounce:
+        bo, bd = bounce_batch(dag, batches[0][1], batches[0][2])
+        batches.append(("bounce", bo, bd))
+    stream = torch.cuda.current_stream()
+    dev_batches = []
+    for label, o, d in batches:
+        to = torch.from_numpy(o).cuda()
+        td = torch.from_numpy(d).cuda()
+        out = cbq.alloc_hits(o.shape[0])
+        f = cbq.count_fetches(dag, to, td).double().mean().item()
+        dev_batches.append((label, to, td, out, f))
+    counter = torch.zeros(1, dtype=torch.int64, device="cuda")
+    rays_per_step = sum(b[1].shape[0] for b in dev_batches)
+
+    def launch(label, to, td, out):
+        if args.kernel == "persistent":
+            cbq.intersect_volume_persistent(dag, to, td, counter, out=out, stream=stream)
+        else:
+            cbq.intersect_volume(dag, to, td, out=out, stream=stream)
+
+    def step(events=None):
+        for i, (label, to, td, out, _) in enumerate(dev_batches):
+            if events is not None:
+                events[i][0].record(stream)
+            launch(label, to, td, out)
+            if events is not None:
+                events[i][1].record(stream)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    per_launch = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                   for _ in dev_batches] for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for k in range(args.steps):
+        step(per_launch[k])
+    t1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    elapsed_ms = max_over_ranks(world, t0.elapsed_time(t1))
+    value = rays_per_step * args.steps * world / (elapsed_ms * 1e-3) / 1e6
+
+    launch_ms = {b[0]: float(np.mean([per_launch[k][i][0].elapsed_time(per_launch[k][i][1])
+                                      for k in range(args.steps)])) for i, b in enumerate(dev_batches)}
+
+    # Roofline of the traversal kernel: algorithmic bytes per launch / launch time.
+    peak, peak_kind = measured_peaks()
+    alg_bytes = {b[0]: b[1].shape[0] * (RAY_BYTES + b[4] * SECTOR + HIT_BYTES) for b in dev_batches}
+    tot_bytes = sum(alg_bytes.values())
+    tot_ms = sum(launch_ms.values())
+    achieved = tot_bytes / (tot_ms * 1e-3) / 1e9
+    l2_stream, l2_rand = cbq.measure_l2(64 << 20, 20)
+    sectors = sum(b[1].shape[0] * b[4] for b in dev_batches)
+    sector_rate = sectors / (tot_ms * 1e-3) / 1e9
+    traffic_per_ray = profiled_traffic(args.workload)
+    roofline = {
+        "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+        "peak_source": f"{peak_kind} hbm_gbs", "kernel": "cbq_k_intersect_" + args.kernel,
+        "traffic": None if traffic_per_ray is None else traffic_per_ray * rays_per_step / len(dev_batches),
+        "bytes_per_ray": {b[0]: RAY_BYTES + b[4] * SECTOR + HIT_BYTES for b in dev_batches},
+        "fetches_per_ray": {b[0]: b[4] for b in dev_batches},
+        "l2": {"achieved_gbs": achieved, "stream_peak_gbs": l2_stream, "frac_stream": achieved / l2_stream,
+               "sector_rate_gsps": sector_rate, "random_sector_peak_gsps": l2_rand,
+               "frac_sector": sector_rate / l2_rand, "peak_source": "cbq_measure_l2 (this run)"},
+    }
+
+    # End to end through the host-buffer C ABI, pinned host memory, copies inside.
+    host = []
+    for label, o, d in batches:
+        po = torch.from_numpy(o).pin_memory()
+        pd = torch.from_numpy(d).pin_memory()
+        n = o.shape[0]
+        outs = {"hit": torch.empty(n, dtype=torch.uint8).pin_memory(),
+                "distance": torch.empty(n, dtype=torch.float32).pin_memory(),
+                "material": torch.empty(n, dtype=torch.int32).pin_memory(),
+                "position": torch.empty((n, 3), dtype=torch.float32).pin_memory(),
+                "normal": torch.empty((n, 3), dtype=torch.float32).pin_memory(),
+                "voxel": torch.empty((n, 3), dtype=torch.int32).pin_memory(),
+                "status": torch.empty(n, dtype=torch.uint8).pin_memory()}
+        host.append((po.numpy(), pd.numpy(), {k: v.numpy() for k, v in outs.items()}))
+
+    def e2e_step():
+        for po, pd, outs in host:
+            cbq.intersect_volume_host(dag, po, pd, out=outs)
+
+    e2e_step()
+    barrier(world)
+    t = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    e2e_s = max_over_ranks(world, time.perf_counter() - t)
+    e2e_value = rays_per_step * args.e2e_steps * world / e2e_s / 1e6
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        dt, kind = cpu_trace(nodes, root, batches)
+        cores = host_cores()
+        cpu = {"value": rays_per_step / dt / 1e6, "unit": "Mrays/s", "cores": cores, "kind": kind,
+               "sample": f"one pass over the full workload ({rays_per_step} rays), {cores} host threads"}
+
+    launches = args.steps * len(dev_batches)
+    line = {
+        "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded scene built by libcbq, generated rays)",
+        "config": {"workload": args.workload, "rays_per_step": rays_per_step, "kernel": args.kernel,
+                   "batches": {b[0]: int(b[1].shape[0]) for b in dev_batches},
+                   "dag_nodes": int(dag.node_count), "dag_bytes": int(dag.bytes),
+                   "l2": "inputs larger than L2 (rays + hits %.0f MB per step); DAG read through L2"
+                         % (rays_per_step * (RAY_BYTES + HIT_BYTES) / 1e6),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "breakdown_mrays": {lbl: b[1].shape[0] / (ms * 1e-3) / 1e6 for (lbl, ms), b in
+                            zip(launch_ms.items(), dev_batches)},
+        "launch_ms": launch_ms,
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": rays_per_step * RAY_BYTES,
+                "d2h_bytes_per_step": rays_per_step * HIT_BYTES},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    dag.destroy()
+
+
+def main():
+    args = parse_args()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gpu(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,421 @@
+"""cubiquity_gb300: GB300-native sparse-voxel-DAG ray traversal.
+
+Python mirror of the C ABI in include/cubiquity_gb300.h (libcbq.so, loaded with
+ctypes).  Names follow the reference's ray-cast interface
+(src/library/raytracing.h): ``find_subdags`` ~ ``findSubDAGs``,
+``intersect_volume`` ~ ``intersectVolume`` (batched), with the same argument
+meaning (``compute_surface_properties``, ``max_footprint``) and the same result
+fields (hit, distance, material, position, normal) plus the integer hit voxel.
+
+There is no CPU fallback: importing this package fails if libcbq.so has not been
+built, and every traversal call runs the CUDA kernels.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+PKG_DIR = Path(__file__).resolve().parent
+LIB_PATH = PKG_DIR / "libcbq.so"
+
+MATERIAL_COUNT = 256
+MAX_FOOTPRINT_DISABLED = -1.0
+QUERY_TMAX = 0x1
+RAY_OK, RAY_ITER_LIMIT, RAY_STUCK = 0, 1, 2
+SCENE_SPHERES, SCENE_TERRAIN, SCENE_CITY = 0, 1, 2
+
+_STATUS = {
+    0: "ok", 1: "invalid argument", 2: "malformed DAG", 3: "out of memory", 4: "CUDA error", 5: "timeout",
+    6: "I/O error", 7: "busy", 8: "not found", 9: "cancelled", 10: "request exceeds capacity", 11: "shut down",
+}
+
+
+class CbqError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        super().__init__(f"{what}: {_STATUS.get(status, 'unknown status')} ({status})")
+
+
+class SubDag(ctypes.Structure):
+    """cbq_subdag: the reference's SubDAG layout (raytracing.h:57-65)."""
+    _fields_ = [("lower_bound", ctypes.c_int32 * 3), ("node_height", ctypes.c_int32),
+                ("padding0", ctypes.c_uint32), ("node_index", ctypes.c_uint32),
+                ("padding1", ctypes.c_uint32), ("padding2", ctypes.c_uint32)]
+
+    def as_tuple(self):
+        return (tuple(self.lower_bound), self.node_height, self.node_index)
+
+
+class _Rays(ctypes.Structure):
+    _fields_ = [("origin_tmax", ctypes.c_void_p), ("direction", ctypes.c_void_p)]
+
+
+class _Hits(ctypes.Structure):
+    _fields_ = [("hit", ctypes.c_void_p), ("distance", ctypes.c_void_p), ("material", ctypes.c_void_p),
+                ("position", ctypes.c_void_p), ("normal", ctypes.c_void_p), ("voxel", ctypes.c_void_p),
+                ("status", ctypes.c_void_p)]
+
+
+class _Query(ctypes.Structure):
+    _fields_ = [("compute_surface", ctypes.c_int32), ("max_footprint", ctypes.c_float),
+                ("flags", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class _DagInfo(ctypes.Structure):
+    _fields_ = [("node_count", ctypes.c_uint64), ("bytes", ctypes.c_uint64), ("root", ctypes.c_uint32),
+                ("max_subdag_height", ctypes.c_int32), ("subdags", SubDag * 8),
+                ("device_nodes", ctypes.c_void_p)]
+
+
+def _load() -> ctypes.CDLL:
+    if not LIB_PATH.exists():
+        raise ImportError(
+            f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+            "(there is no CPU fallback for the traversal)")
+    return ctypes.CDLL(str(LIB_PATH))
+
+
+_lib = _load()
+
+_P = ctypes.c_void_p
+_U64 = ctypes.c_uint64
+_U32 = ctypes.c_uint32
+_I32 = ctypes.c_int32
+
+
+def _sig(name, argtypes, restype=ctypes.c_int):
+    fn = getattr(_lib, name)
+    fn.argtypes = argtypes
+    fn.restype = restype
+    return fn
+
+
+_sig("cbq_status_string", [ctypes.c_int], ctypes.c_char_p)
+_sig("cbq_abi_version", [], ctypes.c_int)
+_sig("cbq_dag_validate", [_P, _U64, _U32])
+_sig("cbq_find_subdags", [_P, _U64, _U32, ctypes.POINTER(SubDag)])
+_sig("cbq_dag_create", [_P, _U64, _U32, ctypes.POINTER(_P)])
+_sig("cbq_dag_destroy", [_P])
+_sig("cbq_dag_get_info", [_P, ctypes.POINTER(_DagInfo)])
+_sig("cbq_dag_set_l2_persistence", [_P, _P, ctypes.c_float])
+_sig("cbq_intersect", [_P, ctypes.POINTER(_Rays), _U64, ctypes.POINTER(_Query), ctypes.POINTER(_Hits), _P])
+_sig("cbq_intersect_host", [_P, _P, _P, _U64, ctypes.POINTER(_Query), ctypes.POINTER(_Hits)])
+_sig("cbq_intersect_persistent", [_P, ctypes.POINTER(_Rays), _U64, ctypes.POINTER(_Query), ctypes.POINTER(_Hits),
+                                  _P, _U32, _P])
+_sig("cbq_count_fetches", [_P, ctypes.POINTER(_Rays), _U64, ctypes.POINTER(_Query), _P, _P])
+_sig("cbq_build_scene", [ctypes.c_int, ctypes.c_int, _U64, ctypes.c_int, ctypes.c_int,
+                         ctypes.POINTER(ctypes.POINTER(ctypes.c_uint32)), ctypes.POINTER(_U64),
+                         ctypes.POINTER(_U32)])
+_sig("cbq_scene_voxels", [ctypes.c_int, ctypes.c_int, _U64, ctypes.c_int, _I32, _I32, _I32, _I32, _I32, _I32, _P])
+_sig("cbq_free", [_P], None)
+_sig("cbq_dag_voxel", [_P, _U64, _U32, _I32, _I32, _I32, ctypes.POINTER(ctypes.c_uint8)])
+_sig("cbq_dag_save", [ctypes.c_char_p, _P, _U64, _U32])
+_sig("cbq_dag_load", [ctypes.c_char_p, ctypes.POINTER(ctypes.POINTER(ctypes.c_uint32)), ctypes.POINTER(_U64),
+                      ctypes.POINTER(_U32)])
+_sig("cbq_dag_reorder_bfs", [_P, _U64, _U32, _P, ctypes.POINTER(_U64), ctypes.POINTER(_U32)])
+_sig("cbq_gen_pinhole_rays", [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.c_double,
+                              _I32, _I32, _P, _P])
+_sig("cbq_gen_bounce_rays", [_P, _P, _U64, _U64, _U64, _P, _P])
+_sig("cbq_measure_l2", [_U64, ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)])
+
+
+def _check(status: int, what: str) -> None:
+    if status != 0:
+        raise CbqError(status, what)
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded libcbq.so (for callers that bind further entry points)."""
+    return _lib
+
+
+def _np_ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data
+
+
+def _nodes_arg(nodes: np.ndarray) -> np.ndarray:
+    nodes = np.ascontiguousarray(nodes, dtype=np.uint32).reshape(-1)
+    if nodes.size % 8 != 0:
+        raise ValueError("node array length must be a multiple of 8")
+    return nodes
+
+
+# ----------------------------------------------------------------- host helpers
+
+def validate(nodes: np.ndarray, root: int) -> None:
+    n = _nodes_arg(nodes)
+    _check(_lib.cbq_dag_validate(_np_ptr(n), n.size // 8, root), "cbq_dag_validate")
+
+
+def find_subdags(nodes: np.ndarray, root: int) -> list[SubDag]:
+    """findSubDAGs (raytracing.cpp:89-97)."""
+    n = _nodes_arg(nodes)
+    out = (SubDag * 8)()
+    _check(_lib.cbq_find_subdags(_np_ptr(n), n.size // 8, root, out), "cbq_find_subdags")
+    return list(out)
+
+
+def _take_malloced(ptr, count_words: int) -> np.ndarray:
+    arr = np.ctypeslib.as_array(ptr, shape=(count_words,)).copy()
+    _lib.cbq_free(ctypes.cast(ptr, ctypes.c_void_p))
+    return arr
+
+
+def build_scene(kind: int, edge_log2: int, seed: int, param: int = 0, threads: int = 0) -> tuple[np.ndarray, int]:
+    """Canonical DAG of a seeded scene; returns (nodes uint32[count*8], root)."""
+    p = ctypes.POINTER(ctypes.c_uint32)()
+    cnt = _U64()
+    root = _U32()
+    _check(_lib.cbq_build_scene(kind, edge_log2, seed, param, threads, ctypes.byref(p), ctypes.byref(cnt),
+                                ctypes.byref(root)), "cbq_build_scene")
+    return _take_malloced(p, cnt.value * 8), root.value
+
+
+def scene_voxels(kind: int, edge_log2: int, seed: int, param: int, lo, size) -> np.ndarray:
+    """Voxel materials of a scene over a box, shape (sz, sy, sx)."""
+    sx, sy, sz = (int(v) for v in size)
+    out = np.empty((sz, sy, sx), dtype=np.uint8)
+    _check(_lib.cbq_scene_voxels(kind, edge_log2, seed, param, int(lo[0]), int(lo[1]), int(lo[2]), sx, sy, sz,
+                                 _np_ptr(out)), "cbq_scene_voxels")
+    return out
+
+
+def dag_voxel(nodes: np.ndarray, root: int, x: int, y: int, z: int) -> int:
+    """Volume::voxel (storage.cpp:481-499)."""
+    n = _nodes_arg(nodes)
+    m = ctypes.c_uint8()
+    _check(_lib.cbq_dag_voxel(_np_ptr(n), n.size // 8, root, x, y, z, ctypes.byref(m)), "cbq_dag_voxel")
+    return m.value
+
+
+def save_dag(path: str | os.PathLike, nodes: np.ndarray, root: int) -> None:
+    n = _nodes_arg(nodes)
+    _check(_lib.cbq_dag_save(os.fsencode(path), _np_ptr(n), n.size // 8, root), "cbq_dag_save")
+
+
+def load_dag(path: str | os.PathLike) -> tuple[np.ndarray, int]:
+    p = ctypes.POINTER(ctypes.c_uint32)()
+    cnt = _U64()
+    root = _U32()
+    _check(_lib.cbq_dag_load(os.fsencode(path), ctypes.byref(p), ctypes.byref(cnt), ctypes.byref(root)),
+           "cbq_dag_load")
+    return _take_malloced(p, cnt.value * 8), root.value
+
+
+def reorder_bfs(nodes: np.ndarray, root: int) -> tuple[np.ndarray, int]:
+    n = _nodes_arg(nodes)
+    out = np.empty_like(n)
+    cnt = _U64()
+    r = _U32()
+    _check(_lib.cbq_dag_reorder_bfs(_np_ptr(n), n.size // 8, root, _np_ptr(out), ctypes.byref(cnt), ctypes.byref(r)),
+           "cbq_dag_reorder_bfs")
+    return out[: cnt.value * 8].copy(), r.value
+
+
+def canonical_hash(nodes: np.ndarray, root: int) -> str:
+    """SHA-256 of the DAG renumbered breadth-first: equal iff the graphs are equal."""
+    import hashlib
+    canon, croot = reorder_bfs(nodes, root)
+    h = hashlib.sha256()
+    h.update(np.uint32(croot).tobytes())
+    h.update(canon.tobytes())
+    return h.hexdigest()
+
+
+def pinhole_rays(eye, target, tan_half_fov: float, width: int, height: int) -> tuple[np.ndarray, np.ndarray]:
+    """Scanline-order pinhole rays as (origin_tmax[n,4], direction[n,4]) float32."""
+    n = width * height
+    o = np.empty((n, 4), dtype=np.float32)
+    d = np.empty((n, 4), dtype=np.float32)
+    e = (ctypes.c_double * 3)(*eye)
+    t = (ctypes.c_double * 3)(*target)
+    _check(_lib.cbq_gen_pinhole_rays(e, t, tan_half_fov, width, height, _np_ptr(o), _np_ptr(d)),
+           "cbq_gen_pinhole_rays")
+    return o, d
+
+
+def bounce_rays(hit_position: np.ndarray, hit_normal: np.ndarray, n: int, seed: int) -> tuple[np.ndarray, np.ndarray]:
+    """Cosine-weighted bounce rays from hit points (pathtracing_demo.cpp:163-166)."""
+    hp = np.ascontiguousarray(hit_position, dtype=np.float32).reshape(-1, 3)
+    hn = np.ascontiguousarray(hit_normal, dtype=np.float32).reshape(-1, 3)
+    o = np.empty((n, 4), dtype=np.float32)
+    d = np.empty((n, 4), dtype=np.float32)
+    _check(_lib.cbq_gen_bounce_rays(_np_ptr(hp), _np_ptr(hn), hp.shape[0], n, seed, _np_ptr(o), _np_ptr(d)),
+           "cbq_gen_bounce_rays")
+    return o, d
+
+
+# --------------------------------------------------------------- device DAG
+
+def measure_l2(working_set_bytes: int = 64 << 20, iterations: int = 20) -> tuple[float, float]:
+    """(streaming L2 read GB/s, random 32-byte-sector reads in Gsectors/s) on the current device."""
+    a = ctypes.c_double()
+    b = ctypes.c_double()
+    _check(_lib.cbq_measure_l2(working_set_bytes, iterations, ctypes.byref(a), ctypes.byref(b)), "cbq_measure_l2")
+    return a.value, b.value
+
+
+HIT_FIELDS = ("hit", "distance", "material", "position", "normal", "voxel", "status")
+
+
+@dataclass
+class Query:
+    compute_surface_properties: bool = True
+    max_footprint: float = MAX_FOOTPRINT_DISABLED
+    use_tmax: bool = False
+
+    def c(self) -> _Query:
+        return _Query(1 if self.compute_surface_properties else 0, float(self.max_footprint),
+                      QUERY_TMAX if self.use_tmax else 0, 0)
+
+
+class Dag:
+    """A DAG resident on the current CUDA device (cbq_dag)."""
+
+    def __init__(self, nodes: np.ndarray, root: int):
+        n = _nodes_arg(nodes)
+        h = _P()
+        _check(_lib.cbq_dag_create(_np_ptr(n), n.size // 8, root, ctypes.byref(h)), "cbq_dag_create")
+        self._h = h
+        info = _DagInfo()
+        _check(_lib.cbq_dag_get_info(h, ctypes.byref(info)), "cbq_dag_get_info")
+        self.node_count = info.node_count
+        self.bytes = info.bytes
+        self.root = info.root
+        self.max_subdag_height = info.max_subdag_height
+        self.subdags = list(info.subdags)
+        self.device_nodes = info.device_nodes
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise RuntimeError("DAG destroyed")
+        return self._h
+
+    def destroy(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            _lib.cbq_dag_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+    def set_l2_persistence(self, fraction: float, stream=None) -> None:
+        _check(_lib.cbq_dag_set_l2_persistence(self.handle, _stream_ptr(stream), fraction),
+               "cbq_dag_set_l2_persistence")
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+def _torch_ptr(t):
+    return None if t is None else t.data_ptr()
+
+
+def alloc_hits(n: int, device="cuda", fields=HIT_FIELDS) -> dict:
+    import torch
+    shapes = {"hit": ((n,), torch.uint8), "distance": ((n,), torch.float32), "material": ((n,), torch.int32),
+              "position": ((n, 3), torch.float32), "normal": ((n, 3), torch.float32),
+              "voxel": ((n, 3), torch.int32), "status": ((n,), torch.uint8)}
+    return {k: torch.empty(*shapes[k][0], dtype=shapes[k][1], device=device) for k in fields}
+
+
+def _hits_struct(out: dict) -> _Hits:
+    return _Hits(*[_torch_ptr(out.get(k)) for k in HIT_FIELDS])
+
+
+def _check_rays_tensor(t, n=None):
+    import torch
+    if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float32 and t.dim() == 2
+            and t.shape[1] == 4 and t.is_contiguous()):
+        raise ValueError("rays must be contiguous float32 CUDA tensors of shape (n, 4)")
+    if n is not None and t.shape[0] != n:
+        raise ValueError("origin and direction arrays differ in length")
+
+
+def intersect_volume(dag: Dag, origin_tmax, direction, compute_surface_properties: bool = True,
+                     max_footprint: float = MAX_FOOTPRINT_DISABLED, use_tmax: bool = False, out: dict | None = None,
+                     stream=None) -> dict:
+    """Batched intersectVolume (raytracing.cpp:397-478) on device tensors.
+
+    origin_tmax, direction: float32 CUDA tensors (n, 4).  Returns a dict of
+    device tensors (see HIT_FIELDS); pass ``out`` to reuse buffers.
+    """
+    _check_rays_tensor(origin_tmax)
+    n = origin_tmax.shape[0]
+    _check_rays_tensor(direction, n)
+    if out is None:
+        out = alloc_hits(n, origin_tmax.device)
+    rays = _Rays(origin_tmax.data_ptr(), direction.data_ptr())
+    q = Query(compute_surface_properties, max_footprint, use_tmax).c()
+    _check(_lib.cbq_intersect(dag.handle, ctypes.byref(rays), n, ctypes.byref(q), ctypes.byref(_hits_struct(out)),
+                              _stream_ptr(stream)), "cbq_intersect")
+    return out
+
+
+def intersect_volume_persistent(dag: Dag, origin_tmax, direction, work_counter, compute_surface_properties=True,
+                                max_footprint=MAX_FOOTPRINT_DISABLED, use_tmax=False, chunk: int = 0,
+                                out: dict | None = None, stream=None) -> dict:
+    """The persistent-warp form; ``work_counter`` is an int64 CUDA tensor (>= 1 element)."""
+    _check_rays_tensor(origin_tmax)
+    n = origin_tmax.shape[0]
+    _check_rays_tensor(direction, n)
+    if out is None:
+        out = alloc_hits(n, origin_tmax.device)
+    rays = _Rays(origin_tmax.data_ptr(), direction.data_ptr())
+    q = Query(compute_surface_properties, max_footprint, use_tmax).c()
+    _check(_lib.cbq_intersect_persistent(dag.handle, ctypes.byref(rays), n, ctypes.byref(q),
+                                         ctypes.byref(_hits_struct(out)), work_counter.data_ptr(), chunk,
+                                         _stream_ptr(stream)), "cbq_intersect_persistent")
+    return out
+
+
+def count_fetches(dag: Dag, origin_tmax, direction, compute_surface_properties=True,
+                  max_footprint=MAX_FOOTPRINT_DISABLED, stream=None):
+    import torch
+    _check_rays_tensor(origin_tmax)
+    n = origin_tmax.shape[0]
+    _check_rays_tensor(direction, n)
+    f = torch.empty(n, dtype=torch.int32, device=origin_tmax.device)
+    rays = _Rays(origin_tmax.data_ptr(), direction.data_ptr())
+    q = Query(compute_surface_properties, max_footprint, False).c()
+    _check(_lib.cbq_count_fetches(dag.handle, ctypes.byref(rays), n, ctypes.byref(q), f.data_ptr(),
+                                  _stream_ptr(stream)), "cbq_count_fetches")
+    return f
+
+
+def alloc_host_hits(n: int) -> dict:
+    return {"hit": np.empty(n, np.uint8), "distance": np.empty(n, np.float32), "material": np.empty(n, np.uint32),
+            "position": np.empty((n, 3), np.float32), "normal": np.empty((n, 3), np.float32),
+            "voxel": np.empty((n, 3), np.int32), "status": np.empty(n, np.uint8)}
+
+
+def intersect_volume_host(dag: Dag, origin_tmax: np.ndarray, direction: np.ndarray,
+                          compute_surface_properties: bool = True, max_footprint: float = MAX_FOOTPRINT_DISABLED,
+                          use_tmax: bool = False, out: dict | None = None) -> dict:
+    """Host-buffer form (cbq_intersect_host): copies in, traverses, copies out."""
+    o = np.ascontiguousarray(origin_tmax, dtype=np.float32).reshape(-1, 4)
+    d = np.ascontiguousarray(direction, dtype=np.float32).reshape(-1, 4)
+    if o.shape != d.shape:
+        raise ValueError("origin and direction arrays differ in length")
+    n = o.shape[0]
+    if out is None:
+        out = alloc_host_hits(n)
+    hits = _Hits(*[_np_ptr(out.get(k)) for k in HIT_FIELDS])
+    q = Query(compute_surface_properties, max_footprint, use_tmax).c()
+    _check(_lib.cbq_intersect_host(dag.handle, _np_ptr(o), _np_ptr(d), n, ctypes.byref(q), ctypes.byref(hits)),
+           "cbq_intersect_host")
+    return out

@@ -1,0 +1,304 @@
+// Device-side C ABI: DAG upload, traversal launches (plain and persistent).
+#include "cbq_internal.hpp"
+#include "cbq_traverse.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+
+using namespace cbq;
+
+namespace {
+
+constexpr int kPlainBlock = 128;
+constexpr int kPersistBlock = 256;
+constexpr uint32_t kDefaultChunk = 64;
+
+dev::DagParams make_dag_params(const cbq_dag* dag)
+{
+    dev::DagParams p;
+    p.nodes = dag->d_nodes;
+    for (int i = 0; i < 8; i++) {
+        p.sd[i].lx = dag->subdags[i].lower_bound[0];
+        p.sd[i].ly = dag->subdags[i].lower_bound[1];
+        p.sd[i].lz = dag->subdags[i].lower_bound[2];
+        p.sd[i].height = dag->subdags[i].node_height;
+        p.sd[i].node = dag->subdags[i].node_index;
+        p.sd[i].pad[0] = p.sd[i].pad[1] = p.sd[i].pad[2] = 0;
+    }
+    return p;
+}
+
+dev::QueryParams make_query(const cbq_query* q)
+{
+    dev::QueryParams p;
+    p.compute_surface = q ? q->compute_surface : 1;
+    p.max_footprint = q ? q->max_footprint : CBQ_MAX_FOOTPRINT_DISABLED;
+    p.flags = q ? q->flags : 0u;
+    return p;
+}
+
+dev::HitsOut make_hits(const cbq_hits* h)
+{
+    dev::HitsOut o;
+    o.hit = h->hit;
+    o.distance = h->distance;
+    o.material = h->material;
+    o.position = h->position;
+    o.normal = h->normal;
+    o.voxel = h->voxel;
+    o.status = h->status;
+    return o;
+}
+
+bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+cbq_status check_rays(const cbq_rays* rays)
+{
+    if (!rays || !rays->origin_tmax || !rays->direction) return CBQ_ERR_INVALID_ARGUMENT;
+    if (!aligned16(rays->origin_tmax) || !aligned16(rays->direction)) return CBQ_ERR_INVALID_ARGUMENT;
+    return CBQ_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Kernels
+// ---------------------------------------------------------------------------
+
+// One ray per thread, stack in local memory.
+__global__ void __launch_bounds__(kPlainBlock) cbq_k_intersect_plain(dev::DagParams dag,
+                                                                     const float4* __restrict__ orig,
+                                                                     const float4* __restrict__ dir, uint64_t n,
+                                                                     dev::QueryParams q, dev::HitsOut out,
+                                                                     uint32_t* __restrict__ fetch_out)
+{
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    dev::LocalStack stack;
+    uint32_t fetches = 0;
+    const dev::RayResult r = dev::intersect_volume(dag, __ldg(orig + i), __ldg(dir + i), q, stack, &fetches);
+    dev::write_result(out, i, r);
+    if (fetch_out) fetch_out[i] = fetches;
+}
+
+// Persistent warps: each warp takes `chunk` rays at a time from an atomic
+// counter; the descent stack lives in shared memory (one column per thread).
+__global__ void __launch_bounds__(kPersistBlock) cbq_k_intersect_persistent(
+    dev::DagParams dag, const float4* __restrict__ orig, const float4* __restrict__ dir, uint64_t n,
+    dev::QueryParams q, dev::HitsOut out, unsigned long long* __restrict__ counter, uint32_t chunk)
+{
+    extern __shared__ uint32_t smem_stack[];
+    dev::SharedStack stack;
+    stack.base = smem_stack + threadIdx.x;
+    stack.stride = blockDim.x;
+    const unsigned lane = threadIdx.x & 31u;
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(counter, (unsigned long long)chunk);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const uint64_t end = min((uint64_t)base + chunk, n);
+        for (uint64_t i = base + lane; i < end; i += 32) {
+            const dev::RayResult r = dev::intersect_volume(dag, __ldg(orig + i), __ldg(dir + i), q, stack,
+                                                           (uint32_t*)nullptr);
+            dev::write_result(out, i, r);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+
+extern "C" {
+
+cbq_status cbq_dag_create(const uint32_t* host_nodes, uint64_t node_count, uint32_t root, cbq_dag** out)
+{
+    if (!out) return CBQ_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    cbq_status st = validate_nodes(host_nodes, node_count, root);
+    if (st != CBQ_OK) return st;
+    cbq_dag* dag = new (std::nothrow) cbq_dag();
+    if (!dag) return CBQ_ERR_OUT_OF_MEMORY;
+    st = find_subdags(host_nodes, node_count, root, dag->subdags);
+    if (st != CBQ_OK) { delete dag; return st; }
+    dag->node_count = node_count;
+    dag->root = root;
+    dag->max_height = 0;
+    for (int i = 0; i < 8; i++)
+        if (dag->subdags[i].node_index > 0) dag->max_height = std::max(dag->max_height, dag->subdags[i].node_height);
+    if (cudaGetDevice(&dag->device) != cudaSuccess) { delete dag; return CBQ_ERR_CUDA; }
+    const size_t bytes = (size_t)node_count * 32u;
+    cudaError_t e = cudaMalloc((void**)&dag->d_nodes, bytes);
+    if (e != cudaSuccess) { cudaGetLastError(); delete dag; return CBQ_ERR_OUT_OF_MEMORY; }
+    e = cudaMemcpy(dag->d_nodes, host_nodes, bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { cudaFree(dag->d_nodes); delete dag; return CBQ_ERR_CUDA; }
+    *out = dag;
+    return CBQ_OK;
+}
+
+cbq_status cbq_dag_destroy(cbq_dag* dag)
+{
+    if (!dag) return CBQ_ERR_INVALID_ARGUMENT;
+    cudaFree(dag->d_nodes);
+    if (dag->d_stage) cudaFree(dag->d_stage);
+    if (dag->d_counter) cudaFree(dag->d_counter);
+    delete dag;
+    return CBQ_OK;
+}
+
+cbq_status cbq_dag_get_info(const cbq_dag* dag, cbq_dag_info* info)
+{
+    if (!dag || !info) return CBQ_ERR_INVALID_ARGUMENT;
+    info->node_count = dag->node_count;
+    info->bytes = dag->node_count * 32u;
+    info->root = dag->root;
+    info->max_subdag_height = dag->max_height;
+    std::memcpy(info->subdags, dag->subdags, sizeof(dag->subdags));
+    info->device_nodes = dag->d_nodes;
+    return CBQ_OK;
+}
+
+cbq_status cbq_dag_set_l2_persistence(const cbq_dag* dag, cbq_stream_t stream, float fraction)
+{
+    if (!dag || fraction < 0.0f || fraction > 1.0f) return CBQ_ERR_INVALID_ARGUMENT;
+    cudaStreamAttrValue attr;
+    std::memset(&attr, 0, sizeof(attr));
+    if (fraction > 0.0f) {
+        int max_window = 0, max_persist = 0;
+        cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, dag->device);
+        cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, dag->device);
+        if (max_window <= 0 || max_persist <= 0) return CBQ_OK;  // not supported: leave caching as is
+        const size_t want = (size_t)((double)max_persist * fraction);
+        if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want) != cudaSuccess) return CBQ_ERR_CUDA;
+        const size_t bytes = (size_t)dag->node_count * 32u;
+        const size_t window = std::min<size_t>(bytes, (size_t)max_window);
+        attr.accessPolicyWindow.base_ptr = dag->d_nodes;
+        attr.accessPolicyWindow.num_bytes = window;
+        attr.accessPolicyWindow.hitRatio = (float)std::min(1.0, (double)want / (double)window);
+        attr.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+        attr.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    }
+    if (cudaStreamSetAttribute((cudaStream_t)stream, cudaStreamAttributeAccessPolicyWindow, &attr) != cudaSuccess)
+        return CBQ_ERR_CUDA;
+    return CBQ_OK;
+}
+
+cbq_status cbq_intersect(const cbq_dag* dag, const cbq_rays* rays, uint64_t n, const cbq_query* query,
+                         const cbq_hits* hits, cbq_stream_t stream)
+{
+    if (!dag || !hits) return CBQ_ERR_INVALID_ARGUMENT;
+    cbq_status st = check_rays(rays);
+    if (st != CBQ_OK) return st;
+    if (n == 0) return CBQ_OK;
+    const uint64_t blocks = (n + kPlainBlock - 1) / kPlainBlock;
+    if (blocks > 0x7fffffffull) return CBQ_ERR_INVALID_ARGUMENT;
+    cbq_k_intersect_plain<<<(unsigned)blocks, kPlainBlock, 0, (cudaStream_t)stream>>>(
+        make_dag_params(dag), (const float4*)rays->origin_tmax, (const float4*)rays->direction, n,
+        make_query(query), make_hits(hits), nullptr);
+    return cudaGetLastError() == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
+}
+
+cbq_status cbq_count_fetches(const cbq_dag* dag, const cbq_rays* rays, uint64_t n, const cbq_query* query,
+                             uint32_t* fetches, cbq_stream_t stream)
+{
+    if (!dag || !fetches) return CBQ_ERR_INVALID_ARGUMENT;
+    cbq_status st = check_rays(rays);
+    if (st != CBQ_OK) return st;
+    if (n == 0) return CBQ_OK;
+    const uint64_t blocks = (n + kPlainBlock - 1) / kPlainBlock;
+    dev::HitsOut none;
+    std::memset(&none, 0, sizeof(none));
+    cbq_k_intersect_plain<<<(unsigned)blocks, kPlainBlock, 0, (cudaStream_t)stream>>>(
+        make_dag_params(dag), (const float4*)rays->origin_tmax, (const float4*)rays->direction, n,
+        make_query(query), none, fetches);
+    return cudaGetLastError() == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
+}
+
+cbq_status cbq_intersect_persistent(const cbq_dag* dag, const cbq_rays* rays, uint64_t n, const cbq_query* query,
+                                    const cbq_hits* hits, uint64_t* work_counter, uint32_t chunk,
+                                    cbq_stream_t stream)
+{
+    if (!dag || !hits || !work_counter) return CBQ_ERR_INVALID_ARGUMENT;
+    cbq_status st = check_rays(rays);
+    if (st != CBQ_OK) return st;
+    if (n == 0) return CBQ_OK;
+    if (chunk == 0) chunk = kDefaultChunk;
+    const int stack_h = std::max(1, (int)dag->max_height);
+    const size_t smem = (size_t)stack_h * kPersistBlock * sizeof(uint32_t);
+    int sms = 0, per_sm = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dag->device) != cudaSuccess) return CBQ_ERR_CUDA;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cbq_k_intersect_persistent, kPersistBlock, smem) !=
+        cudaSuccess)
+        return CBQ_ERR_CUDA;
+    per_sm = std::max(per_sm, 1);
+    if (cudaMemsetAsync(work_counter, 0, sizeof(uint64_t), (cudaStream_t)stream) != cudaSuccess) return CBQ_ERR_CUDA;
+    cbq_k_intersect_persistent<<<sms * per_sm, kPersistBlock, smem, (cudaStream_t)stream>>>(
+        make_dag_params(dag), (const float4*)rays->origin_tmax, (const float4*)rays->direction, n,
+        make_query(query), make_hits(hits), (unsigned long long*)work_counter, chunk);
+    return cudaGetLastError() == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
+}
+
+cbq_status cbq_intersect_host(const cbq_dag* cdag, const float* host_origin_tmax, const float* host_direction,
+                              uint64_t n, const cbq_query* query, const cbq_hits* host_hits)
+{
+    if (!cdag || !host_origin_tmax || !host_direction || !host_hits) return CBQ_ERR_INVALID_ARGUMENT;
+    if (n == 0) return CBQ_OK;
+    cbq_dag* dag = const_cast<cbq_dag*>(cdag);
+    std::lock_guard<std::mutex> lock(dag->staging_lock);
+    // Per ray: 32 B in, 46 B out (hit, distance, material, position, normal, voxel, status).
+    const size_t per_ray = 32 + 1 + 4 + 4 + 12 + 12 + 12 + 1;
+    if (n > dag->stage_capacity) {
+        if (dag->d_stage) cudaFree(dag->d_stage);
+        dag->d_stage = nullptr;
+        dag->stage_capacity = 0;
+        if (cudaMalloc(&dag->d_stage, (size_t)n * per_ray + 256) != cudaSuccess) {
+            cudaGetLastError();
+            return CBQ_ERR_OUT_OF_MEMORY;
+        }
+        dag->stage_capacity = n;
+    }
+    char* p = (char*)dag->d_stage;
+    float* d_o = (float*)p;
+    p += n * 16;
+    float* d_d = (float*)p;
+    p += n * 16;
+    cbq_hits dh;
+    dh.position = (float*)p; p += n * 12;
+    dh.normal = (float*)p; p += n * 12;
+    dh.voxel = (int32_t*)p; p += n * 12;
+    dh.distance = (float*)p; p += n * 4;
+    dh.material = (uint32_t*)p; p += n * 4;
+    dh.hit = (uint8_t*)p; p += n;
+    dh.status = (uint8_t*)p;
+    cudaStream_t s = 0;
+    if (cudaMemcpyAsync(d_o, host_origin_tmax, n * 16, cudaMemcpyHostToDevice, s) != cudaSuccess) return CBQ_ERR_CUDA;
+    if (cudaMemcpyAsync(d_d, host_direction, n * 16, cudaMemcpyHostToDevice, s) != cudaSuccess) return CBQ_ERR_CUDA;
+    cbq_hits launch = dh;
+    if (!host_hits->hit) launch.hit = nullptr;
+    if (!host_hits->distance) launch.distance = nullptr;
+    if (!host_hits->material) launch.material = nullptr;
+    if (!host_hits->position) launch.position = nullptr;
+    if (!host_hits->normal) launch.normal = nullptr;
+    if (!host_hits->voxel) launch.voxel = nullptr;
+    if (!host_hits->status) launch.status = nullptr;
+    cbq_rays rays{d_o, d_d};
+    cbq_status st = cbq_intersect(dag, &rays, n, query, &launch, (cbq_stream_t)s);
+    if (st != CBQ_OK) return st;
+    struct Copy { void* dst; const void* src; size_t bytes; };
+    const Copy copies[] = {
+        {host_hits->hit, launch.hit, n}, {host_hits->distance, launch.distance, n * 4},
+        {host_hits->material, launch.material, n * 4}, {host_hits->position, launch.position, n * 12},
+        {host_hits->normal, launch.normal, n * 12}, {host_hits->voxel, launch.voxel, n * 12},
+        {host_hits->status, launch.status, n}};
+    for (const Copy& c : copies) {
+        if (!c.dst) continue;
+        if (cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess) return CBQ_ERR_CUDA;
+    }
+    return cudaStreamSynchronize(s) == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
+}
+
+}  // extern "C"

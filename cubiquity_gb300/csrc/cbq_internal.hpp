@@ -1,0 +1,35 @@
+// Internal declarations shared by the host (.cpp) and device (.cu) parts of
+// libcbq.  Not part of the public ABI.
+#pragma once
+
+#include "../../include/cubiquity_gb300.h"
+
+#include <cstdint>
+#include <mutex>
+
+namespace cbq {
+
+// Host-side findSubDAGs (raytracing.cpp:43-97).  Returns CBQ_ERR_BAD_DAG if a
+// followed index is out of range.
+cbq_status find_subdags(const uint32_t* nodes, uint64_t node_count, uint32_t root, cbq_subdag out[8]);
+
+// Full structural check of a host node array.
+cbq_status validate_nodes(const uint32_t* nodes, uint64_t node_count, uint32_t root);
+
+}  // namespace cbq
+
+// The opaque DAG handle.
+struct cbq_dag {
+    uint32_t* d_nodes = nullptr;   // device, node_count * 8 words
+    uint64_t node_count = 0;
+    uint32_t root = 0;
+    cbq_subdag subdags[8];
+    int32_t max_height = 0;        // max SubDAG height (stack depth)
+    int device = 0;
+
+    // Staging for cbq_intersect_host.
+    std::mutex staging_lock;
+    void* d_stage = nullptr;
+    uint64_t stage_capacity = 0;   // rays
+    uint64_t* d_counter = nullptr;
+};

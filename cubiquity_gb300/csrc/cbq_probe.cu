@@ -1,0 +1,91 @@
+// L2 bandwidth probes: the roofline denominators for the traversal, whose node
+// fetches are 32-byte L2 sectors rather than streaming HBM reads.
+#include "cbq_internal.hpp"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+namespace {
+
+// Streaming read of an L2-resident buffer, 16 bytes per thread per step.
+__global__ void __launch_bounds__(256) cbq_k_l2_stream(const uint4* __restrict__ buf, uint64_t n16, int iters,
+                                                       uint32_t* __restrict__ sink)
+{
+    uint32_t acc = 0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (int it = 0; it < iters; it++) {
+        for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += stride) {
+            const uint4 v = __ldcg(buf + i);
+            acc ^= v.x ^ v.y ^ v.z ^ v.w;
+        }
+    }
+    if (acc == 0x9e3779b9u) sink[0] = acc;  // keeps the loads alive
+}
+
+// Independent random 4-byte reads, one 32-byte sector each, 8 in flight per thread.
+__global__ void __launch_bounds__(256) cbq_k_l2_random(const uint32_t* __restrict__ buf, uint32_t mask_words,
+                                                       int iters, uint32_t* __restrict__ sink)
+{
+    uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) * 2654435761u + 12345u;
+    uint32_t acc = 0;
+    for (int it = 0; it < iters; it++) {
+        uint32_t idx[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            s ^= s << 13;
+            s ^= s >> 17;
+            s ^= s << 5;
+            idx[k] = (s & mask_words) & ~7u;
+        }
+#pragma unroll
+        for (int k = 0; k < 8; k++) acc += __ldcg(buf + idx[k]);
+    }
+    if (acc == 0x9e3779b9u) sink[0] = acc;
+}
+
+}  // namespace
+
+extern "C" cbq_status cbq_measure_l2(uint64_t working_set_bytes, int iterations, double* stream_gbs,
+                                     double* random_gsectors_per_s)
+{
+    if (!stream_gbs || !random_gsectors_per_s || iterations <= 0) return CBQ_ERR_INVALID_ARGUMENT;
+    // Power-of-two working set (for the random probe's mask), at least 1 MiB.
+    uint64_t ws = 1u << 20;
+    while (ws * 2 <= working_set_bytes) ws *= 2;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return CBQ_ERR_CUDA;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    void* buf = nullptr;
+    uint32_t* sink = nullptr;
+    if (cudaMalloc(&buf, ws) != cudaSuccess) { cudaGetLastError(); return CBQ_ERR_OUT_OF_MEMORY; }
+    if (cudaMalloc((void**)&sink, 64) != cudaSuccess) { cudaFree(buf); cudaGetLastError(); return CBQ_ERR_OUT_OF_MEMORY; }
+    cudaMemset(buf, 0x5a, ws);
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    const int grid = sms * 8;
+    // Warm the L2 with one pass, then time `iterations` passes.
+    cbq_k_l2_stream<<<grid, 256>>>((const uint4*)buf, ws / 16, 1, sink);
+    cudaEventRecord(a);
+    cbq_k_l2_stream<<<grid, 256>>>((const uint4*)buf, ws / 16, iterations, sink);
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    *stream_gbs = (double)ws * iterations / (ms * 1e-3) / 1e9;
+    const int rand_iters = 64;
+    cbq_k_l2_random<<<grid, 256>>>((const uint32_t*)buf, (uint32_t)(ws / 4 - 1), 4, sink);
+    cudaEventRecord(a);
+    cbq_k_l2_random<<<grid, 256>>>((const uint32_t*)buf, (uint32_t)(ws / 4 - 1), rand_iters, sink);
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    cudaEventElapsedTime(&ms, a, b);
+    const double loads = (double)grid * 256 * rand_iters * 8;
+    *random_gsectors_per_s = loads / (ms * 1e-3) / 1e9;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(buf);
+    cudaFree(sink);
+    return cudaGetLastError() == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
+}

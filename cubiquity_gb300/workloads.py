@@ -1,0 +1,89 @@
+"""Seeded synthetic workloads for the traversal (scenes + rays).
+
+The reference publishes no dataset for this path (its sample .dag files are a
+download), so these seeded scenes stand in, with the shapes and sizes of the
+benchmark configurations:
+
+  spheres-256   256^3, 64 spheres (centres in [32,224]^3, radii 8..40,
+                material 1 + i mod 7, first sphere wins) over a ground slab z<32
+                of material 8; 1024x1024 pinhole at (-128,-128,300) looking at
+                (128,128,128), 60 degree vertical fov: 1,048,576 primary rays.
+  terrain-4096  4096^3 fBm value-noise terrain (6 octaves, base period 1024,
+                gain 0.5, heights in [512,2048]) with caves where 3D value noise
+                (period 128) > 0.35 and 16 materials banded by height;
+                2048x2048 primary rays plus 4,194,304 cosine-weighted bounce
+                rays from the primary hits (origin offset 0.01 along the normal).
+
+Everything is generated by libcbq (C++), so the same inputs come out on every
+machine: ray generation uses only + - * / sqrt in double precision.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+import cubiquity_gb300 as cbq
+
+TAN_30 = 0.57735026918962576451  # tan(60 degrees / 2)
+
+
+@dataclass(frozen=True)
+class SceneSpec:
+    kind: int
+    edge_log2: int
+    seed: int
+    param: int = 0
+
+    def build(self, threads: int = 0):
+        return cbq.build_scene(self.kind, self.edge_log2, self.seed, self.param, threads)
+
+    def voxels(self, lo, size):
+        return cbq.scene_voxels(self.kind, self.edge_log2, self.seed, self.param, lo, size)
+
+
+@dataclass(frozen=True)
+class CameraSpec:
+    eye: tuple
+    target: tuple
+    width: int
+    height: int
+    tan_half_fov: float = TAN_30
+
+    def rays(self):
+        return cbq.pinhole_rays(self.eye, self.target, self.tan_half_fov, self.width, self.height)
+
+
+SPHERES_256 = SceneSpec(cbq.SCENE_SPHERES, 8, 20240607, 64)
+SPHERES_256_CAMERA = CameraSpec((-128.0, -128.0, 300.0), (128.0, 128.0, 128.0), 1024, 1024)
+
+TERRAIN_4096 = SceneSpec(cbq.SCENE_TERRAIN, 12, 4096001)
+TERRAIN_4096_CAMERA = CameraSpec((-1024.0, -1024.0, 3072.0), (2048.0, 2048.0, 1024.0), 2048, 2048)
+TERRAIN_BOUNCE_SEED = 0xB0B0C0DE
+
+
+def terrain_scaled(edge_log2: int, seed: int = 4096001) -> SceneSpec:
+    return SceneSpec(cbq.SCENE_TERRAIN, edge_log2, seed)
+
+
+def camera_scaled(edge_log2: int, width: int, height: int) -> CameraSpec:
+    """The terrain camera of TERRAIN_4096_CAMERA scaled to an edge of 2^edge_log2."""
+    s = (1 << edge_log2) / 4096.0
+    return CameraSpec(tuple(v * s for v in TERRAIN_4096_CAMERA.eye), tuple(v * s for v in TERRAIN_4096_CAMERA.target),
+                      width, height)
+
+
+def bounce_from_hits(hits: dict, n: int, seed: int = TERRAIN_BOUNCE_SEED):
+    """Bounce rays from the hits of a primary pass (host arrays or tensors)."""
+    hit = _np(hits["hit"]).astype(bool)
+    pos = _np(hits["position"])[hit]
+    nrm = _np(hits["normal"])[hit]
+    if pos.shape[0] == 0:
+        raise ValueError("no primary hits to bounce from")
+    return cbq.bounce_rays(pos, nrm, n, seed)
+
+
+def _np(a):
+    if isinstance(a, np.ndarray):
+        return a
+    return a.detach().cpu().numpy()

@@ -1,0 +1,223 @@
+/*
+ * cubiquity_gb300 — GB300 (sm_103a) sparse-voxel-DAG ray traversal, C ABI.
+ *
+ * A drop-in for Cubiquity's ray cast (src/library/raytracing.h:48-81): the same
+ * flat node store, the same eight SubDAG virtual roots, the same ray -> hit
+ * semantics (hit flag, distance, material, position, normal), bit-exact, plus an
+ * integer hit voxel.  All entry points return a cbq_status and never throw.
+ *
+ * Conventions
+ *   - "device" pointers are CUDA global-memory pointers on the current device;
+ *     "host" pointers are CPU memory (pinned memory is faster but not required).
+ *   - Rays are two arrays of float4 (16-byte aligned, 16 bytes per ray):
+ *       origin_tmax[i] = (ox, oy, oz, tmax)   direction[i] = (dx, dy, dz, unused)
+ *     tmax is read only when CBQ_QUERY_TMAX is set in cbq_query.flags.
+ *   - Outputs are per-field arrays; any pointer may be NULL to skip that field.
+ *     position / normal / voxel hold three values per ray (x, y, z interleaved).
+ *   - Launching calls are stream-ordered and asynchronous on `stream`
+ *     (a cudaStream_t; NULL = legacy default stream).
+ *   - A cbq_dag is immutable once created and may be used from several host
+ *     threads and streams at once.
+ */
+#ifndef CUBIQUITY_GB300_H
+#define CUBIQUITY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CBQ_ABI_VERSION 1
+
+typedef struct CUstream_st* cbq_stream_t; /* identical to cudaStream_t */
+
+typedef enum cbq_status {
+    CBQ_OK = 0,
+    CBQ_ERR_INVALID_ARGUMENT = 1,
+    CBQ_ERR_BAD_DAG = 2,          /* child index out of range, bad root, bad file */
+    CBQ_ERR_OUT_OF_MEMORY = 3,
+    CBQ_ERR_CUDA = 4,
+    CBQ_ERR_TIMEOUT = 5,
+    CBQ_ERR_IO = 6,
+    CBQ_ERR_BUSY = 7,
+    CBQ_ERR_NOT_FOUND = 8,
+    CBQ_ERR_CANCELLED = 9,
+    CBQ_ERR_CAPACITY = 10,        /* request larger than the server can ever admit */
+    CBQ_ERR_SHUTDOWN = 11
+} cbq_status;
+
+/* Per-ray status values written to cbq_hits.status. */
+#define CBQ_RAY_OK 0u
+#define CBQ_RAY_ITER_LIMIT 1u  /* more than CBQ_MAX_RAY_FETCHES node fetches: reported as a miss */
+#define CBQ_RAY_STUCK 2u       /* an advance step that moved nowhere (NaN slab): reported as a miss */
+#define CBQ_MAX_RAY_FETCHES (1u << 17)
+
+#define CBQ_MATERIAL_COUNT 256u
+#define CBQ_MAX_FOOTPRINT_DISABLED (-1.0f) /* raytracing.h:71 */
+
+/* Same 32-byte layout as the reference's SubDAG (raytracing.h:57-65) and its
+ * std430 GLSL twin (pathtracing.frag SSBO 1). */
+typedef struct cbq_subdag {
+    int32_t lower_bound[3];
+    int32_t node_height;
+    uint32_t padding0;
+    uint32_t node_index;
+    uint32_t padding1, padding2;
+} cbq_subdag;
+
+typedef struct cbq_rays {
+    const float* origin_tmax; /* 4 floats per ray */
+    const float* direction;   /* 4 floats per ray */
+} cbq_rays;
+
+typedef struct cbq_hits {
+    uint8_t* hit;
+    float* distance;          /* FP32; the reference widens the same value to double */
+    uint32_t* material;
+    float* position;          /* 3 per ray */
+    float* normal;            /* 3 per ray */
+    int32_t* voxel;           /* 3 per ray: floor(position - 0.5*normal + 0.5) */
+    uint8_t* status;          /* CBQ_RAY_* */
+} cbq_hits;
+
+#define CBQ_QUERY_TMAX 0x1u   /* a hit with distance > tmax is reported as a miss */
+
+typedef struct cbq_query {
+    int32_t compute_surface;  /* intersectVolume's computeSurfaceProperties */
+    float max_footprint;      /* intersectVolume's maxFootprint (LOD); -1 disables */
+    uint32_t flags;           /* CBQ_QUERY_* */
+    uint32_t reserved;
+} cbq_query;
+
+typedef struct cbq_dag cbq_dag;
+
+typedef struct cbq_dag_info {
+    uint64_t node_count;      /* including the 256 material slots */
+    uint64_t bytes;           /* node_count * 32 */
+    uint32_t root;
+    int32_t max_subdag_height;
+    cbq_subdag subdags[8];
+    const uint32_t* device_nodes;
+} cbq_dag_info;
+
+/* ---------------------------------------------------------------- basics */
+
+const char* cbq_status_string(cbq_status s);
+int cbq_abi_version(void);
+
+/* Checks that every child index (and the root) is < node_count and that slots
+ * 0..255 are material nodes.  Host memory. */
+cbq_status cbq_dag_validate(const uint32_t* nodes, uint64_t node_count, uint32_t root);
+
+/* findSubDAGs (raytracing.h:69 / raytracing.cpp:89-97) on a host node array. */
+cbq_status cbq_find_subdags(const uint32_t* nodes, uint64_t node_count, uint32_t root,
+                            cbq_subdag out[8]);
+
+/* ------------------------------------------------------------ DAG store */
+
+/* Validates, computes the SubDAGs and uploads the node store to the current
+ * device as one flat uint32 array (the buffer the reference binds as SSBO 0,
+ * gpu_pathtracing_viewer.cpp:43-57).  Replaces Volume + findSubDAGs for the
+ * device path.  Synchronous. */
+cbq_status cbq_dag_create(const uint32_t* host_nodes, uint64_t node_count, uint32_t root,
+                          cbq_dag** out);
+cbq_status cbq_dag_destroy(cbq_dag* dag);
+cbq_status cbq_dag_get_info(const cbq_dag* dag, cbq_dag_info* info);
+
+/* Sets a persisting-L2 access-policy window over the node store on `stream`
+ * (fraction of the device's persisting-L2 limit to reserve, 0 disables). */
+cbq_status cbq_dag_set_l2_persistence(const cbq_dag* dag, cbq_stream_t stream, float fraction);
+
+/* ------------------------------------------------------------ traversal */
+
+/* intersectVolume (raytracing.h:72-76 / raytracing.cpp:397-478) for n rays:
+ * one launch, device rays in, device hits out.  The plain drop-in form. */
+cbq_status cbq_intersect(const cbq_dag* dag, const cbq_rays* rays, uint64_t n,
+                         const cbq_query* query, const cbq_hits* hits, cbq_stream_t stream);
+
+/* As cbq_intersect, with HOST rays and HOST hits: copies in, traverses, copies
+ * out, and waits for completion.  Allocates and caches device staging buffers
+ * per dag (serialised by a per-dag lock). */
+cbq_status cbq_intersect_host(const cbq_dag* dag, const float* host_origin_tmax,
+                              const float* host_direction, uint64_t n, const cbq_query* query,
+                              const cbq_hits* host_hits);
+
+/* Persistent form: a grid sized to the device's SMs whose warps pull chunks of
+ * `chunk` rays from an atomic work counter.  `work_counter` is caller-owned
+ * device scratch (one uint64, zeroed by this call on `stream`).  chunk = 0
+ * selects the tuned default. */
+cbq_status cbq_intersect_persistent(const cbq_dag* dag, const cbq_rays* rays, uint64_t n,
+                                    const cbq_query* query, const cbq_hits* hits,
+                                    uint64_t* work_counter, uint32_t chunk, cbq_stream_t stream);
+
+/* Statistics form of cbq_intersect: writes only the number of node fetches
+ * (dependent child loads) each ray performed to the device array `fetches`. */
+cbq_status cbq_count_fetches(const cbq_dag* dag, const cbq_rays* rays, uint64_t n,
+                             const cbq_query* query, uint32_t* fetches, cbq_stream_t stream);
+
+/* Diagnostic (no reference counterpart): on the current device, measures the
+ * streaming read bandwidth of an L2-resident buffer of about working_set_bytes
+ * (GB/s) and the rate of independent random 32-byte-sector reads within it
+ * (Gsectors/s).  These are the roofline denominators of the traversal, whose
+ * node fetches are L2 sectors.  Synchronous. */
+cbq_status cbq_measure_l2(uint64_t working_set_bytes, int iterations, double* stream_gbs,
+                          double* random_gsectors_per_s);
+
+/* ---------------------------------------------------- workload generators */
+
+typedef enum cbq_scene_kind {
+    CBQ_SCENE_SPHERES = 0, /* param = sphere count */
+    CBQ_SCENE_TERRAIN = 1,
+    CBQ_SCENE_CITY = 2
+} cbq_scene_kind;
+
+/* Builds the canonical DAG of a seeded scene of edge 2^edge_log2 at the origin
+ * (the same DAG Volume::setVoxel + bake would reach).  *nodes_out is malloc'd;
+ * release with cbq_free.  threads <= 0 uses all cores. */
+cbq_status cbq_build_scene(cbq_scene_kind kind, int edge_log2, uint64_t seed, int param, int threads,
+                           uint32_t** nodes_out, uint64_t* node_count_out, uint32_t* root_out);
+
+/* Evaluates the scene's voxels over the box [x0, x0+sx) x [y0, y0+sy) x [z0, z0+sz)
+ * into out (x fastest). */
+cbq_status cbq_scene_voxels(cbq_scene_kind kind, int edge_log2, uint64_t seed, int param,
+                            int32_t x0, int32_t y0, int32_t z0, int32_t sx, int32_t sy, int32_t sz,
+                            uint8_t* out);
+
+void cbq_free(void* p);
+
+/* Volume::voxel (storage.cpp:481-499) on a host node array. */
+cbq_status cbq_dag_voxel(const uint32_t* nodes, uint64_t node_count, uint32_t root, int32_t x,
+                         int32_t y, int32_t z, uint8_t* material);
+
+/* The reference .dag format (storage.cpp:192-206, 505-542):
+ * u32 root | u32 internal_count | internal_count * 32 bytes (material slots omitted). */
+cbq_status cbq_dag_save(const char* path, const uint32_t* nodes, uint64_t node_count, uint32_t root);
+cbq_status cbq_dag_load(const char* path, uint32_t** nodes_out, uint64_t* node_count_out,
+                        uint32_t* root_out);
+
+/* Renumbers the reachable internal nodes in breadth-first order from the root
+ * (material slots keep 0..255); the graph is unchanged.  out_nodes must hold
+ * node_count * 8 words; *out_count receives the reachable count. */
+cbq_status cbq_dag_reorder_bfs(const uint32_t* nodes, uint64_t node_count, uint32_t root,
+                               uint32_t* out_nodes, uint64_t* out_count, uint32_t* out_root);
+
+/* Pinhole camera rays in scanline order, computed in double precision with
+ * + - * / sqrt only (identical on every platform) and rounded to float.
+ * tan_half_fov = tan(vertical fov / 2); z is up. */
+cbq_status cbq_gen_pinhole_rays(const double eye[3], const double target[3], double tan_half_fov,
+                                int32_t width, int32_t height, float* origin_tmax, float* direction);
+
+/* Cosine-weighted bounce rays: ray i starts at hit (i mod hit_count) at
+ * position + 0.01 * normal (pathtracing_demo.cpp:166) with direction
+ * normalize(normal + u), u uniform on the unit sphere from a counter-based hash
+ * of (seed, i). */
+cbq_status cbq_gen_bounce_rays(const float* hit_position, const float* hit_normal, uint64_t hit_count,
+                               uint64_t n, uint64_t seed, float* origin_tmax, float* direction);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUBIQUITY_GB300_H */

@@ -1,0 +1,224 @@
+"""Parity of the CUDA path (through the C ABI) with the reference and the oracle.
+
+Bar: hit, material, voxel and status bit-exact; distance, position and normal
+are also required bit-exact here (the kernel performs the reference's FP32
+operations in the reference's order), which is stricter than the 1e-5
+relative tolerance the path is specified with.
+"""
+import hashlib
+
+import numpy as np
+import pytest
+
+import cubiquity_gb300 as cbq
+from cubiquity_gb300 import workloads as W
+from conftest import subdags_of
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+FIELDS = ("hit", "distance", "material", "position", "normal", "voxel")
+QUERIES = {"surface": (True, -1.0), "nosurface": (False, -1.0), "lod": (True, 0.05)}
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _device():
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    torch.cuda.set_device(0)
+
+
+def _dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _host(out):
+    return {k: v.cpu().numpy() for k, v in out.items()}
+
+
+def _bits_equal(a, b):
+    a = np.ascontiguousarray(a)
+    b = np.ascontiguousarray(b)
+    return a.shape == b.shape and np.array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
+def _assert_same(got, want, fields=FIELDS, what=""):
+    for k in fields:
+        g = got[k]
+        w = want[k]
+        if k == "material":
+            g, w = g.astype(np.uint32), w.astype(np.uint32)
+        if k == "distance":
+            w = w.astype(np.float32)
+        if not _bits_equal(g, w):
+            bad = np.nonzero((g != w).reshape(g.shape[0], -1).any(axis=1))[0]
+            raise AssertionError(f"{what} {k}: {bad.size} rays differ, first {bad[:10].tolist()}")
+
+
+def _digest(out):
+    res = {}
+    for k in FIELDS:
+        a = out[k]
+        if k == "material":
+            a = a.astype(np.uint32)
+        res[k] = hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+    res["hits"] = int(out["hit"].sum())
+    return res
+
+
+@pytest.mark.parametrize("query", list(QUERIES))
+def test_gpu_matches_reference_golden(golden, query):
+    name, fx = golden
+    cs, mf = QUERIES[query]
+    dag = cbq.Dag(fx["nodes"], int(fx["root"]))
+    assert [s.as_tuple() for s in dag.subdags] == subdags_of(fx)
+    out = _host(cbq.intersect_volume(dag, _dev(fx["origin_tmax"]), _dev(fx["direction"]), cs, mf))
+    assert not out["status"].any()
+    _assert_same(out, {k: fx[f"{query}_{k}"] for k in FIELDS}, what=f"{name}/{query}")
+
+
+def test_gpu_full_spheres256_matches_reference_digest(digests, orc):
+    dg = digests["spheres256"]
+    nodes, root = W.SPHERES_256.build()
+    assert cbq.canonical_hash(nodes, root) == dg["canonical_dag_sha256"]
+    o, d = W.SPHERES_256_CAMERA.rays()
+    dag = cbq.Dag(nodes, root)
+    out = _host(cbq.intersect_volume(dag, _dev(o), _dev(d), True, -1.0))
+    assert _digest(out) == dg["surface"]
+    lod = _host(cbq.intersect_volume(dag, _dev(o), _dev(d), True, dg["lod_max_footprint"]))
+    assert _digest(lod) == dg["lod"]
+    # and ray by ray against the oracle
+    _assert_same(out, orc.intersect(nodes, orc.find_subdags(nodes, root), o, d), what="spheres256")
+
+
+@pytest.fixture(scope="module")
+def terrain():
+    nodes, root = W.TERRAIN_4096.build()
+    dag = cbq.Dag(nodes, root)
+    o, d = W.TERRAIN_4096_CAMERA.rays()
+    yield nodes, root, dag, o, d
+    dag.destroy()
+
+
+def test_gpu_full_terrain4096_matches_reference_digest(terrain, digests, orc):
+    nodes, root, dag, o, d = terrain
+    dg = digests["terrain4096"]
+    assert cbq.canonical_hash(nodes, root) == dg["canonical_dag_sha256"]
+    prim = _host(cbq.intersect_volume(dag, _dev(o), _dev(d)))
+    assert _digest(prim) == dg["primary"]
+    bo, bd = W.bounce_from_hits(prim, o.shape[0])
+    assert hashlib.sha256(bo.tobytes() + bd.tobytes()).hexdigest() == dg["bounce_rays_sha256"]
+    boun = _host(cbq.intersect_volume(dag, _dev(bo), _dev(bd)))
+    assert _digest(boun) == dg["bounce"]
+    sd = orc.find_subdags(nodes, root)
+    _assert_same(prim, orc.intersect(nodes, sd, o, d), what="terrain primary")
+    _assert_same(boun, orc.intersect(nodes, sd, bo, bd), what="terrain bounce")
+
+
+@pytest.mark.parametrize("chunk", [0, 32, 96])
+def test_persistent_equals_plain(terrain, chunk):
+    nodes, root, dag, o, d = terrain
+    to, td = _dev(o), _dev(d)
+    a = _host(cbq.intersect_volume(dag, to, td))
+    ctr = torch.zeros(1, dtype=torch.int64, device="cuda")
+    b = _host(cbq.intersect_volume_persistent(dag, to, td, ctr, chunk=chunk))
+    _assert_same(b, a, FIELDS + ("status",), what=f"persistent chunk={chunk}")
+
+
+def test_host_api_equals_device_api(terrain):
+    nodes, root, dag, o, d = terrain
+    n = 300_001  # not a multiple of any block size
+    a = _host(cbq.intersect_volume(dag, _dev(o[:n]), _dev(d[:n])))
+    b = cbq.intersect_volume_host(dag, o[:n], d[:n])
+    _assert_same(b, a, FIELDS + ("status",), what="host api")
+    c = cbq.intersect_volume_host(dag, o[:1000], d[:1000])  # reuses the cached staging buffers
+    _assert_same(c, {k: v[:1000] for k, v in a.items()}, FIELDS, what="host api reuse")
+
+
+def test_fetch_counts_match_oracle(terrain, orc):
+    nodes, root, dag, o, d = terrain
+    n = 200_000
+    f = cbq.count_fetches(dag, _dev(o[:n]), _dev(d[:n])).cpu().numpy().astype(np.uint32)
+    want = orc.count_fetches(nodes, orc.find_subdags(nodes, root), o[:n], d[:n])
+    assert np.array_equal(f, want)
+
+
+def test_tmax_post_filter(terrain, orc):
+    nodes, root, dag, o, d = terrain
+    n = 100_000
+    o2 = o[:n].copy()
+    o2[:, 3] = np.random.default_rng(1).uniform(0, 6000, n).astype(np.float32)
+    out = _host(cbq.intersect_volume(dag, _dev(o2), _dev(d[:n]), use_tmax=True))
+    want = orc.intersect(nodes, orc.find_subdags(nodes, root), o2, d[:n], use_tmax=True)
+    _assert_same(out, want, what="tmax")
+    full = _host(cbq.intersect_volume(dag, _dev(o2), _dev(d[:n])))
+    assert out["hit"].sum() < full["hit"].sum()
+
+
+def test_null_fields_and_empty_batch(terrain):
+    nodes, root, dag, o, d = terrain
+    n = 5000
+    full = _host(cbq.intersect_volume(dag, _dev(o[:n]), _dev(d[:n])))
+    part = cbq.alloc_hits(n, fields=("voxel", "material"))
+    cbq.intersect_volume(dag, _dev(o[:n]), _dev(d[:n]), out=part)
+    assert np.array_equal(part["voxel"].cpu().numpy(), full["voxel"])
+    assert np.array_equal(part["material"].cpu().numpy(), full["material"])
+    empty = torch.empty((0, 4), dtype=torch.float32, device="cuda")
+    cbq.intersect_volume(dag, empty, empty)
+    torch.cuda.synchronize()
+
+
+def test_misaligned_rays_rejected(terrain):
+    nodes, root, dag, o, d = terrain
+    buf = _dev(np.zeros(4 * 65, np.float32))
+    rays = cbq._Rays(buf.data_ptr() + 4, buf.data_ptr())
+    q = cbq.Query().c()
+    hits = cbq._Hits()
+    st = cbq.lib().cbq_intersect(dag.handle, rays, 64, q, hits, None)
+    assert st == 1
+
+
+def degenerate_rays(n=2000, seed=5):
+    """Zero direction components with origins on, beside and between voxel
+    faces.  Where an origin lies exactly on an axis plane with a zero direction
+    component, 0/0 makes the octant distances NaN and the reference's octant
+    loop (raytracing.cpp:441-475) never advances: those rays end with
+    CBQ_RAY_STUCK on both sides here."""
+    rng = np.random.default_rng(seed)
+    o = np.zeros((n, 4), np.float32)
+    d = np.zeros((n, 4), np.float32)
+    o[:, :3] = np.floor(rng.uniform(0, 64, (n, 3))) + rng.choice([0.5, 0.25, 0.0, -0.5], (n, 3))
+    o[:, 3] = np.inf
+    v = rng.normal(size=(n, 3))
+    v[rng.random((n, 3)) < 0.4] = 0
+    v[(v == 0).all(1), 0] = 1
+    d[:, :3] = v / np.linalg.norm(v, axis=1, keepdims=True)
+    return o, d
+
+
+def test_degenerate_rays_and_stuck_status(orc):
+    nodes, root = W.SceneSpec(cbq.SCENE_SPHERES, 6, 11, 16).build()
+    o, d = degenerate_rays()
+    want = orc.intersect(nodes, orc.find_subdags(nodes, root), o, d)
+    assert (want["status"] == cbq.RAY_STUCK).sum() > 0
+    dag = cbq.Dag(nodes, root)
+    got = _host(cbq.intersect_volume(dag, _dev(o), _dev(d)))
+    _assert_same(got, want, FIELDS + ("status",), what="degenerate")
+
+
+def test_iteration_cap_on_malformed_dag(orc):
+    """An internal node whose children are all empty never occurs in a baked
+    DAG; findNearestMaterial would spin on it.  The fetch cap ends the ray with
+    CBQ_RAY_ITER_LIMIT (bounded: at most 2^22 fetches)."""
+    nodes, root = W.SceneSpec(cbq.SCENE_SPHERES, 6, 11, 16).build()
+    nodes = nodes.copy()
+    empty_node = nodes.size // 8
+    nodes = np.concatenate([nodes, np.zeros(8, np.uint32)])
+    # Route every child of the sub-DAG root to the all-empty node.
+    sd = cbq.find_subdags(nodes, root)[7]
+    nodes[8 * sd.node_index: 8 * sd.node_index + 8] = empty_node
+    o, d = W.CameraSpec((-40.0, -40.0, 90.0), (32.0, 32.0, 32.0), 4, 4).rays()
+    want = orc.intersect(nodes, orc.find_subdags(nodes, root), o, d, True, 0.5)
+    dag = cbq.Dag(nodes, root)
+    got = _host(cbq.intersect_volume(dag, _dev(o), _dev(d), True, 0.5))
+    _assert_same(got, want, FIELDS + ("status",), what="iteration cap")
