@@ -51,7 +51,10 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     p.add_argument("--workload", choices=["terrain-4096", "spheres-256"], default="terrain-4096")
-    p.add_argument("--kernel", choices=["plain", "persistent"], default="plain")
+    p.add_argument("--kernel", choices=["auto", "flat", "nested"], default="auto")
+    p.add_argument("--persistent", action="store_true", help="persistent grid pulling rays from a work counter")
+    p.add_argument("--block", type=int, default=0)
+    p.add_argument("--chunk", type=int, default=0, help="persistent: refill threshold (flat) / grab size (nested)")
     p.add_argument("--e2e-steps", type=int, default=5)
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
@@ -269,6 +272,11 @@ def run_gpu(args, world, rank, local):
     torch.cuda.set_device(local)
     nodes, root, batches, bounce = make_workload(args.workload)
     dag = cbq.Dag(nodes, root)
+    kernel_id = {"auto": cbq.KERNEL_AUTO, "flat": cbq.KERNEL_FLAT, "nested": cbq.KERNEL_NESTED}[args.kernel]
+    dag.set_launch_config(kernel_id, args.block, args.chunk if not args.persistent else 0, 0)
+    cfg = dag.launch_config()
+    kernel_name = ("cbq_k_flat" if cfg["kernel"] == cbq.KERNEL_FLAT else
+                   ("cbq_k_intersect_persistent" if args.persistent else "cbq_k_intersect_plain"))
     if bounce:
         bo, bd = bounce_batch(dag, batches[0][1], batches[0][2])
         batches.append(("bounce", bo, bd))
@@ -284,8 +292,8 @@ def run_gpu(args, world, rank, local):
     rays_per_step = sum(b[1].shape[0] for b in dev_batches)
 
     def launch(label, to, td, out):
-        if args.kernel == "persistent":
-            cbq.intersect_volume_persistent(dag, to, td, counter, out=out, stream=stream)
+        if args.persistent:
+            cbq.intersect_volume_persistent(dag, to, td, counter, chunk=args.chunk, out=out, stream=stream)
         else:
             cbq.intersect_volume(dag, to, td, out=out, stream=stream)
 
@@ -334,7 +342,7 @@ def run_gpu(args, world, rank, local):
     traffic_per_ray = profiled_traffic(args.workload)
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-        "peak_source": f"{peak_kind} hbm_gbs", "kernel": "cbq_k_intersect_" + args.kernel,
+        "peak_source": f"{peak_kind} hbm_gbs", "kernel": kernel_name,
         "traffic": None if traffic_per_ray is None else traffic_per_ray * rays_per_step / len(dev_batches),
         "bytes_per_ray": {b[0]: RAY_BYTES + b[4] * SECTOR + HIT_BYTES for b in dev_batches},
         "fetches_per_ray": {b[0]: b[4] for b in dev_batches},
@@ -383,7 +391,8 @@ def run_gpu(args, world, rank, local):
         "warmup": max(3, args.warmup), "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded scene built by libcbq, generated rays)",
-        "config": {"workload": args.workload, "rays_per_step": rays_per_step, "kernel": args.kernel,
+        "config": {"workload": args.workload, "rays_per_step": rays_per_step, "kernel": kernel_name,
+                   "persistent": bool(args.persistent), "launch_config": cfg,
                    "batches": {b[0]: int(b[1].shape[0]) for b in dev_batches},
                    "dag_nodes": int(dag.node_count), "dag_bytes": int(dag.bytes),
                    "l2": "inputs larger than L2 (rays + hits %.0f MB per step); DAG read through L2"

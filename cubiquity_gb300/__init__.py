@@ -65,6 +65,18 @@ class _Query(ctypes.Structure):
                 ("flags", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
+KERNEL_AUTO, KERNEL_NESTED, KERNEL_FLAT = 0, 1, 2
+
+
+class LaunchConfig(ctypes.Structure):
+    """cbq_launch_config."""
+    _fields_ = [("kernel", ctypes.c_int32), ("block", ctypes.c_int32), ("chunk", ctypes.c_uint32),
+                ("refill_min", ctypes.c_uint32)]
+
+    def as_dict(self):
+        return {"kernel": self.kernel, "block": self.block, "chunk": self.chunk, "refill_min": self.refill_min}
+
+
 class _DagInfo(ctypes.Structure):
     _fields_ = [("node_count", ctypes.c_uint64), ("bytes", ctypes.c_uint64), ("root", ctypes.c_uint32),
                 ("max_subdag_height", ctypes.c_int32), ("subdags", SubDag * 8),
@@ -102,6 +114,8 @@ _sig("cbq_dag_create", [_P, _U64, _U32, ctypes.POINTER(_P)])
 _sig("cbq_dag_destroy", [_P])
 _sig("cbq_dag_get_info", [_P, ctypes.POINTER(_DagInfo)])
 _sig("cbq_dag_set_l2_persistence", [_P, _P, ctypes.c_float])
+_sig("cbq_dag_set_launch_config", [_P, ctypes.POINTER(LaunchConfig)])
+_sig("cbq_dag_get_launch_config", [_P, ctypes.POINTER(LaunchConfig)])
 _sig("cbq_intersect", [_P, ctypes.POINTER(_Rays), _U64, ctypes.POINTER(_Query), ctypes.POINTER(_Hits), _P])
 _sig("cbq_intersect_host", [_P, _P, _P, _U64, ctypes.POINTER(_Query), ctypes.POINTER(_Hits)])
 _sig("cbq_intersect_persistent", [_P, ctypes.POINTER(_Rays), _U64, ctypes.POINTER(_Query), ctypes.POINTER(_Hits),
@@ -306,6 +320,16 @@ class Dag:
             self.destroy()
         except Exception:
             pass
+
+    def set_launch_config(self, kernel: int = KERNEL_AUTO, block: int = 0, chunk: int = 0,
+                          refill_min: int = 0) -> None:
+        cfg = LaunchConfig(kernel, block, chunk, refill_min)
+        _check(_lib.cbq_dag_set_launch_config(self.handle, ctypes.byref(cfg)), "cbq_dag_set_launch_config")
+
+    def launch_config(self) -> dict:
+        cfg = LaunchConfig()
+        _check(_lib.cbq_dag_get_launch_config(self.handle, ctypes.byref(cfg)), "cbq_dag_get_launch_config")
+        return cfg.as_dict()
 
     def set_l2_persistence(self, fraction: float, stream=None) -> None:
         _check(_lib.cbq_dag_set_l2_persistence(self.handle, _stream_ptr(stream), fraction),

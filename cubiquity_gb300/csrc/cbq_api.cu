@@ -10,7 +10,25 @@
 
 using namespace cbq;
 
+namespace cbq {
+bool float_positions_exact(const cbq_dag* dag);
+cbq_status launch_flat(const cbq_dag* dag, const dev::DagParams& dp, const dev::QueryParams& q,
+                       const dev::HitsOut& out, const float4* orig, const float4* dir, uint64_t n,
+                       uint32_t* fetch_out, bool persistent, uint64_t* counter, int block, uint32_t refill_min,
+                       cudaStream_t stream);
+}  // namespace cbq
+
 namespace {
+
+constexpr int kFlatBlockDefault = 128;
+constexpr uint32_t kRefillDefault = 8;
+
+bool use_flat(const cbq_dag* dag)
+{
+    return dag->flat_ok && dag->cfg.kernel != CBQ_KERNEL_NESTED;
+}
+
+int flat_block(const cbq_dag* dag) { return dag->cfg.block > 0 ? dag->cfg.block : kFlatBlockDefault; }
 
 constexpr int kPlainBlock = 128;
 constexpr int kPersistBlock = 256;
@@ -124,7 +142,9 @@ cbq_status cbq_dag_create(const uint32_t* host_nodes, uint64_t node_count, uint3
     cbq_dag* dag = new (std::nothrow) cbq_dag();
     if (!dag) return CBQ_ERR_OUT_OF_MEMORY;
     st = find_subdags(host_nodes, node_count, root, dag->subdags);
+    if (st == CBQ_OK) st = validate_heights(host_nodes, node_count, dag->subdags);
     if (st != CBQ_OK) { delete dag; return st; }
+    dag->flat_ok = float_positions_exact(dag);
     dag->node_count = node_count;
     dag->root = root;
     dag->max_height = 0;
@@ -194,12 +214,37 @@ cbq_status cbq_intersect(const cbq_dag* dag, const cbq_rays* rays, uint64_t n, c
     cbq_status st = check_rays(rays);
     if (st != CBQ_OK) return st;
     if (n == 0) return CBQ_OK;
+    if (use_flat(dag))
+        return launch_flat(dag, make_dag_params(dag), make_query(query), make_hits(hits),
+                           (const float4*)rays->origin_tmax, (const float4*)rays->direction, n, nullptr, false,
+                           nullptr, flat_block(dag), 0u, (cudaStream_t)stream);
     const uint64_t blocks = (n + kPlainBlock - 1) / kPlainBlock;
     if (blocks > 0x7fffffffull) return CBQ_ERR_INVALID_ARGUMENT;
     cbq_k_intersect_plain<<<(unsigned)blocks, kPlainBlock, 0, (cudaStream_t)stream>>>(
         make_dag_params(dag), (const float4*)rays->origin_tmax, (const float4*)rays->direction, n,
         make_query(query), make_hits(hits), nullptr);
     return cudaGetLastError() == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
+}
+
+cbq_status cbq_dag_set_launch_config(cbq_dag* dag, const cbq_launch_config* cfg)
+{
+    if (!dag || !cfg) return CBQ_ERR_INVALID_ARGUMENT;
+    if (cfg->kernel < CBQ_KERNEL_AUTO || cfg->kernel > CBQ_KERNEL_FLAT) return CBQ_ERR_INVALID_ARGUMENT;
+    if (cfg->block < 0 || cfg->block > 256 || (cfg->block % 32) != 0) return CBQ_ERR_INVALID_ARGUMENT;
+    if (cfg->refill_min > 32) return CBQ_ERR_INVALID_ARGUMENT;
+    dag->cfg = *cfg;
+    return CBQ_OK;
+}
+
+cbq_status cbq_dag_get_launch_config(const cbq_dag* dag, cbq_launch_config* cfg)
+{
+    if (!dag || !cfg) return CBQ_ERR_INVALID_ARGUMENT;
+    *cfg = dag->cfg;
+    if (cfg->kernel == CBQ_KERNEL_AUTO) cfg->kernel = dag->flat_ok ? CBQ_KERNEL_FLAT : CBQ_KERNEL_NESTED;
+    if (cfg->block == 0) cfg->block = use_flat(dag) ? kFlatBlockDefault : kPlainBlock;
+    if (cfg->chunk == 0) cfg->chunk = kDefaultChunk;
+    if (cfg->refill_min == 0) cfg->refill_min = kRefillDefault;
+    return CBQ_OK;
 }
 
 cbq_status cbq_count_fetches(const cbq_dag* dag, const cbq_rays* rays, uint64_t n, const cbq_query* query,
@@ -209,9 +254,13 @@ cbq_status cbq_count_fetches(const cbq_dag* dag, const cbq_rays* rays, uint64_t 
     cbq_status st = check_rays(rays);
     if (st != CBQ_OK) return st;
     if (n == 0) return CBQ_OK;
-    const uint64_t blocks = (n + kPlainBlock - 1) / kPlainBlock;
     dev::HitsOut none;
     std::memset(&none, 0, sizeof(none));
+    if (use_flat(dag))
+        return launch_flat(dag, make_dag_params(dag), make_query(query), none, (const float4*)rays->origin_tmax,
+                           (const float4*)rays->direction, n, fetches, false, nullptr, flat_block(dag), 0u,
+                           (cudaStream_t)stream);
+    const uint64_t blocks = (n + kPlainBlock - 1) / kPlainBlock;
     cbq_k_intersect_plain<<<(unsigned)blocks, kPlainBlock, 0, (cudaStream_t)stream>>>(
         make_dag_params(dag), (const float4*)rays->origin_tmax, (const float4*)rays->direction, n,
         make_query(query), none, fetches);
@@ -226,7 +275,14 @@ cbq_status cbq_intersect_persistent(const cbq_dag* dag, const cbq_rays* rays, ui
     cbq_status st = check_rays(rays);
     if (st != CBQ_OK) return st;
     if (n == 0) return CBQ_OK;
-    if (chunk == 0) chunk = kDefaultChunk;
+    if (use_flat(dag)) {
+        const uint32_t refill = chunk ? std::min<uint32_t>(chunk, 32u)
+                                      : (dag->cfg.refill_min ? dag->cfg.refill_min : kRefillDefault);
+        return launch_flat(dag, make_dag_params(dag), make_query(query), make_hits(hits),
+                           (const float4*)rays->origin_tmax, (const float4*)rays->direction, n, nullptr, true,
+                           work_counter, flat_block(dag), refill, (cudaStream_t)stream);
+    }
+    if (chunk == 0) chunk = dag->cfg.chunk ? dag->cfg.chunk : kDefaultChunk;
     const int stack_h = std::max(1, (int)dag->max_height);
     const size_t smem = (size_t)stack_h * kPersistBlock * sizeof(uint32_t);
     int sms = 0, per_sm = 0;

@@ -1,0 +1,284 @@
+// Flat ("while-while") form of the ESVO traversal for sm_103a.
+//
+// The reference's control flow (raytracing.cpp:397-478 around :213-371) is two
+// nested loops with early exits: an octant walk, and inside it the ESVO
+// descend/advance/pop loop.  Run per thread as written, the lanes of a warp
+// leave those loops at different times and drift apart (measured: 1.8-2.8
+// active lanes per instruction).  Here the same arithmetic is re-expressed as a
+// per-lane state machine driven by a single loop: every iteration each lane
+// performs at most one ESVO step (plus any octant transitions), so the warp
+// reconverges at the top of every iteration.  In the persistent form, lanes
+// whose ray is done pull new rays from a global counter (warp-aggregated).
+//
+// Floating-point operations are those of cbq_traverse.cuh / the reference, in
+// the same order (compile with -fmad=false).  Positions are carried both as
+// i32 (for the XOR/MSB pop logic) and as float copies updated by exact float
+// additions; the host only selects this form when every SubDAG's reflected
+// coordinates lie within +-2^24, where (float)(a + b) == (float)a + (float)b.
+#pragma once
+
+#include "cbq_traverse.cuh"
+
+namespace cbq {
+namespace dev {
+
+enum : uint32_t { kLaneIdle = 0u, kLaneEnter = 1u, kLaneNext = 2u, kLaneWalk = 3u };
+
+struct Lane {
+    float4 o, d;                 // the ray as given (o.w = tmax)
+    float rox, roy, roz;         // reflected origin
+    float ix, iy, iz;            // 1 / |dir|
+    float ddx, ddy, ddz;         // octant walk distances (distToOrigin)
+    uint32_t sign, oct;
+    // ESVO walk state
+    uint32_t node, cid, written;
+    int32_t cx, cy, cz, cns;
+    float fx, fy, fz, fcns;
+    int h, start_h;
+    float last_exit;
+    uint32_t fetches, status, mode;
+    uint64_t ray;
+};
+
+struct FlatCtx {
+    DagParams dag;
+    QueryParams q;
+    HitsOut out;
+    const float4* __restrict__ orig;
+    const float4* __restrict__ dir;
+    uint32_t* __restrict__ fetch_out;
+};
+
+__device__ __forceinline__ uint32_t first_child_f(const Lane& L, float entry, float fcx, float fcy, float fcz)
+{
+    const float mx = (fcx - L.rox) * L.ix;
+    const float my = (fcy - L.roy) * L.iy;
+    const float mz = (fcz - L.roz) * L.iz;
+    uint32_t id = (mx < entry ? 1u : 0u) | (my < entry ? 2u : 0u) | (mz < entry ? 4u : 0u);
+    if (entry <= 0.0f) {
+        id |= (L.rox >= fcx ? 1u : 0u) | (L.roy >= fcy ? 2u : 0u) | (L.roz >= fcz ? 4u : 0u);
+    }
+    return id;
+}
+
+// Per-ray set-up: intersectVolume up to the octant loop (raytracing.cpp:409-434).
+__device__ __forceinline__ void lane_begin(Lane& L, const FlatCtx& c, uint64_t i)
+{
+    L.ray = i;
+    L.o = __ldg(c.orig + i);
+    L.d = __ldg(c.dir + i);
+    const uint32_t sbx = L.d.x < 0.0f, sby = L.d.y < 0.0f, sbz = L.d.z < 0.0f;
+    L.sign = sbx | (sby << 1) | (sbz << 2);
+    const float sx = sbx ? -1.0f : 1.0f, sy = sby ? -1.0f : 1.0f, sz = sbz ? -1.0f : 1.0f;
+    L.rox = __fmul_rn(__fadd_rn(L.o.x, 0.5f), sx);
+    L.roy = __fmul_rn(__fadd_rn(L.o.y, 0.5f), sy);
+    L.roz = __fmul_rn(__fadd_rn(L.o.z, 0.5f), sz);
+    const float rdx = fabsf(L.d.x), rdy = fabsf(L.d.y), rdz = fabsf(L.d.z);
+    L.ix = 1.0f / rdx;
+    L.iy = 1.0f / rdy;
+    L.iz = 1.0f / rdz;
+    L.oct = 0u;
+    L.ddx = (-L.rox) / rdx;
+    L.ddy = (-L.roy) / rdy;
+    L.ddz = (-L.roz) / rdz;
+    if (L.ddx < 0.0f) { L.oct += 1u; L.ddx = __fadd_rn(L.ddx, FLT_MAX); }
+    if (L.ddy < 0.0f) { L.oct += 2u; L.ddy = __fadd_rn(L.ddy, FLT_MAX); }
+    if (L.ddz < 0.0f) { L.oct += 4u; L.ddz = __fadd_rn(L.ddz, FLT_MAX); }
+    L.fetches = 0u;
+    L.status = kRayOk;
+    L.mode = kLaneEnter;
+}
+
+// Writes the result of ray L.ray and frees the lane.
+__device__ __forceinline__ void lane_finish(Lane& L, const FlatCtx& c, bool hit, float dist, uint32_t material,
+                                            float nx, float ny, float nz)
+{
+    RayResult r;
+    r.hit = hit;
+    r.distance = hit ? dist : 0.0f;
+    r.material = hit ? material : 0u;
+    r.nx = hit ? nx : 0.0f;
+    r.ny = hit ? ny : 0.0f;
+    r.nz = hit ? nz : 0.0f;
+    r.px = r.py = r.pz = 0.0f;
+    if (hit) {
+        r.px = __fadd_rn(L.o.x, __fmul_rn(L.d.x, dist));
+        r.py = __fadd_rn(L.o.y, __fmul_rn(L.d.y, dist));
+        r.pz = __fadd_rn(L.o.z, __fmul_rn(L.d.z, dist));
+    }
+    r.status = L.status;
+    if ((c.q.flags & 1u) && r.hit && !(r.distance <= L.o.w)) {
+        r.hit = false;
+        r.distance = 0.0f;
+        r.material = 0u;
+        r.px = r.py = r.pz = 0.0f;
+        r.nx = r.ny = r.nz = 0.0f;
+    }
+    write_result(c.out, L.ray, r);
+    if (c.fetch_out) c.fetch_out[L.ray] = L.fetches;
+    L.mode = kLaneIdle;
+}
+
+// One octant transition (raytracing.cpp:469-475).
+__device__ __forceinline__ void lane_next(Lane& L, const FlatCtx& c)
+{
+    const float md = min3_ref(L.ddx, L.ddy, L.ddz);
+    const uint32_t before = L.oct;
+    if (L.ddx <= md) { L.oct += 1u; L.ddx = __fadd_rn(L.ddx, FLT_MAX); }
+    if (L.ddy <= md) { L.oct += 2u; L.ddy = __fadd_rn(L.ddy, FLT_MAX); }
+    if (L.ddz <= md) { L.oct += 4u; L.ddz = __fadd_rn(L.ddz, FLT_MAX); }
+    if (L.oct == before) {  // NaN distances: the reference would revisit this octant forever
+        L.status = kRayStuck;
+        lane_finish(L, c, false, 0.0f, 0u, 0.0f, 0.0f, 0.0f);
+    } else if (L.oct > 7u) {
+        lane_finish(L, c, false, 0.0f, 0u, 0.0f, 0.0f, 0.0f);
+    } else {
+        L.mode = kLaneEnter;
+    }
+}
+
+// Enters the SubDAG of the current octant: the slab test and set-up at the top
+// of intersectRayNodeESVO (raytracing.cpp:218-250, 443-460).
+__device__ __forceinline__ void lane_enter(Lane& L, const FlatCtx& c)
+{
+    const SubDag& s = c.dag.sd[L.oct ^ L.sign];
+    if (s.node == 0u) {
+        L.mode = kLaneNext;
+        return;
+    }
+    const uint32_t sbx = L.sign & 1u, sby = (L.sign >> 1) & 1u, sbz = (L.sign >> 2) & 1u;
+    const uint32_t ns = 1u << s.height;
+    const int32_t px = (int32_t)((sbx ? 0u - (uint32_t)s.lx : (uint32_t)s.lx) - (sbx ? ns : 0u));
+    const int32_t py = (int32_t)((sby ? 0u - (uint32_t)s.ly : (uint32_t)s.ly) - (sby ? ns : 0u));
+    const int32_t pz = (int32_t)((sbz ? 0u - (uint32_t)s.lz : (uint32_t)s.lz) - (sbz ? ns : 0u));
+    const float fpx = (float)px, fpy = (float)py, fpz = (float)pz, fns = (float)ns;
+    const float t0x = (fpx - L.rox) * L.ix;
+    const float t0y = (fpy - L.roy) * L.iy;
+    const float t0z = (fpz - L.roz) * L.iz;
+    const float t1x = ((fpx + fns) - L.rox) * L.ix;
+    const float t1y = ((fpy + fns) - L.roy) * L.iy;
+    const float t1z = ((fpz + fns) - L.roz) * L.iz;
+    const float entry = max3_ref(t0x, t0y, t0z);
+    const float exit_ = min3_ref(t1x, t1y, t1z);
+    if (!(entry < exit_)) {
+        L.mode = kLaneNext;
+        return;
+    }
+    L.start_h = s.height;
+    L.h = s.height;
+    L.node = s.node;
+    L.cns = (int32_t)(ns >> 1);
+    L.fcns = (float)L.cns;
+    L.cid = first_child_f(L, entry, fpx + L.fcns, fpy + L.fcns, fpz + L.fcns);
+    L.cx = px + ((L.cid & 1u) ? L.cns : 0);
+    L.cy = py + ((L.cid & 2u) ? L.cns : 0);
+    L.cz = pz + ((L.cid & 4u) ? L.cns : 0);
+    L.fx = fpx + ((L.cid & 1u) ? L.fcns : 0.0f);
+    L.fy = fpy + ((L.cid & 2u) ? L.fcns : 0.0f);
+    L.fz = fpz + ((L.cid & 4u) ? L.fcns : 0.0f);
+    L.last_exit = exit_;
+    L.written = 0u;
+    L.mode = kLaneWalk;
+}
+
+// One iteration of the ESVO loop (raytracing.cpp:253-367).
+template <typename Stack>
+__device__ __forceinline__ void lane_walk(Lane& L, const FlatCtx& c, Stack& stack)
+{
+    const float c1x = ((L.fx + L.fcns) - L.rox) * L.ix;
+    const float c1y = ((L.fy + L.fcns) - L.roy) * L.iy;
+    const float c1z = ((L.fz + L.fcns) - L.roz) * L.iz;
+    const float tcx = min3_ref(c1x, c1y, c1z);
+    if (L.fetches >= kMaxFetches) {
+        L.status = kRayIterLimit;
+        lane_finish(L, c, false, 0.0f, 0u, 0.0f, 0.0f, 0.0f);
+        return;
+    }
+    const uint32_t child = load_child(c.dag.nodes, L.node, L.cid ^ L.sign);
+    L.fetches++;
+    if (child > 0u) {
+        const float c0x = (L.fx - L.rox) * L.ix;
+        const float c0y = (L.fy - L.roy) * L.iy;
+        const float c0z = (L.fz - L.roz) * L.iz;
+        const float tce = max3_ref(c0x, c0y, c0z);
+        if (child >= kMaterialCount && large_footprint(L.cns, tcx, c.q.max_footprint)) {
+            if (tcx < L.last_exit) {
+                stack.put(L.h, L.node);
+                L.written |= 1u << L.h;
+            }
+            L.last_exit = tcx;
+            L.h--;
+            L.node = child;
+            L.cns >>= 1;
+            L.fcns = (float)L.cns;
+            L.cid = first_child_f(L, tce, L.fx + L.fcns, L.fy + L.fcns, L.fz + L.fcns);
+            if (L.cid & 1u) { L.cx += L.cns; L.fx += L.fcns; }
+            if (L.cid & 2u) { L.cy += L.cns; L.fy += L.fcns; }
+            if (L.cid & 4u) { L.cz += L.cns; L.fz += L.fcns; }
+        } else {
+            uint32_t material = 0u;
+            float nx = 0.0f, ny = 0.0f, nz = 0.0f;
+            if (c.q.compute_surface) {
+                material = nearest_material(c.dag.nodes, child, L.sign, L.fetches, L.status);
+                if (L.status != kRayOk) {
+                    lane_finish(L, c, false, 0.0f, 0u, 0.0f, 0.0f, 0.0f);
+                    return;
+                }
+                nx = __fmul_rn(tce == c0x ? 1.0f : 0.0f, (L.sign & 1u) ? 1.0f : -1.0f);
+                ny = __fmul_rn(tce == c0y ? 1.0f : 0.0f, (L.sign & 2u) ? 1.0f : -1.0f);
+                nz = __fmul_rn(tce == c0z ? 1.0f : 0.0f, (L.sign & 4u) ? 1.0f : -1.0f);
+            }
+            lane_finish(L, c, true, tce, material, nx, ny, nz);
+        }
+        return;
+    }
+    const uint32_t flips = (c1x <= tcx ? 1u : 0u) | (c1y <= tcx ? 2u : 0u) | (c1z <= tcx ? 4u : 0u);
+    if (flips == 0u) {
+        L.status = kRayStuck;
+        lane_finish(L, c, false, 0.0f, 0u, 0.0f, 0.0f, 0.0f);
+        return;
+    }
+    L.cid ^= flips;
+    const int32_t ox = L.cx, oy = L.cy, oz = L.cz;
+    if (flips & 1u) { L.cx += L.cns; L.fx += L.fcns; }
+    if (flips & 2u) { L.cy += L.cns; L.fy += L.fcns; }
+    if (flips & 4u) { L.cz += L.cns; L.fz += L.fcns; }
+    if ((L.cid & flips) != flips) {
+        const uint32_t diff = (uint32_t)(ox ^ L.cx) | (uint32_t)(oy ^ L.cy) | (uint32_t)(oz ^ L.cz);
+        const int msb = 31 - __clz(diff);
+        const int h = msb + 1;
+        if (h > L.start_h) {  // left the sub-DAG: on to the next octant
+            L.mode = kLaneNext;
+            return;
+        }
+        L.h = h;
+        L.node = (L.written & (1u << h)) ? stack.get(h) : 0u;
+        L.cns = (int32_t)(1u << msb);
+        L.fcns = (float)L.cns;
+        L.cid = (uint32_t)((L.cx >> msb) & 1) | ((uint32_t)((L.cy >> msb) & 1) << 1) |
+                ((uint32_t)((L.cz >> msb) & 1) << 2);
+        L.cx = (int32_t)((uint32_t)(L.cx >> h) << h) + ((L.cid & 1u) ? L.cns : 0);
+        L.cy = (int32_t)((uint32_t)(L.cy >> h) << h) + ((L.cid & 2u) ? L.cns : 0);
+        L.cz = (int32_t)((uint32_t)(L.cz >> h) << h) + ((L.cid & 4u) ? L.cns : 0);
+        L.fx = (float)L.cx;
+        L.fy = (float)L.cy;
+        L.fz = (float)L.cz;
+        L.last_exit = 0.0f;
+    }
+}
+
+// Octant transitions until the lane walks a SubDAG or has finished.  Bounded:
+// every kLaneNext raises `oct` (or finishes the ray), every kLaneEnter walks or
+// moves on, so at most 16 transitions happen.
+__device__ __forceinline__ void lane_settle(Lane& L, const FlatCtx& c)
+{
+    while (L.mode == kLaneEnter || L.mode == kLaneNext) {
+        if (L.mode == kLaneNext)
+            lane_next(L, c);
+        else
+            lane_enter(L, c);
+    }
+}
+
+}  // namespace dev
+}  // namespace cbq

@@ -62,6 +62,27 @@ cbq_status validate_nodes(const uint32_t* nodes, uint64_t node_count, uint32_t r
     return CBQ_OK;
 }
 
+cbq_status validate_heights(const uint32_t* nodes, uint64_t node_count, const cbq_subdag subdags[8])
+{
+    // Heights (0..31) at which each internal node has been reached.
+    std::vector<uint32_t> seen(node_count, 0u);
+    std::vector<std::pair<uint32_t, int>> todo;
+    for (int k = 0; k < 8; k++)
+        if (subdags[k].node_index >= kMaterialCount) todo.emplace_back(subdags[k].node_index, subdags[k].node_height);
+    while (!todo.empty()) {
+        const auto [n, h] = todo.back();
+        todo.pop_back();
+        if (h <= 0) return CBQ_ERR_BAD_DAG;  // an internal node where only voxels can be
+        if (seen[n] & (1u << h)) continue;
+        seen[n] |= 1u << h;
+        for (int k = 0; k < 8; k++) {
+            const uint32_t c = nodes[(uint64_t)n * 8 + k];
+            if (c >= kMaterialCount) todo.emplace_back(c, h - 1);
+        }
+    }
+    return CBQ_OK;
+}
+
 }  // namespace cbq
 
 using namespace cbq;
@@ -91,7 +112,12 @@ int cbq_abi_version(void) { return CBQ_ABI_VERSION; }
 
 cbq_status cbq_dag_validate(const uint32_t* nodes, uint64_t node_count, uint32_t root)
 {
-    return validate_nodes(nodes, node_count, root);
+    cbq_status st = validate_nodes(nodes, node_count, root);
+    if (st != CBQ_OK) return st;
+    cbq_subdag sd[8];
+    st = find_subdags(nodes, node_count, root, sd);
+    if (st != CBQ_OK) return st;
+    return validate_heights(nodes, node_count, sd);
 }
 
 cbq_status cbq_find_subdags(const uint32_t* nodes, uint64_t node_count, uint32_t root, cbq_subdag out[8])

@@ -16,6 +16,10 @@ cbq_status find_subdags(const uint32_t* nodes, uint64_t node_count, uint32_t roo
 // Full structural check of a host node array.
 cbq_status validate_nodes(const uint32_t* nodes, uint64_t node_count, uint32_t root);
 
+// Checks that no internal node is reachable from a SubDAG root at height 0
+// (which also excludes cycles), so a traversal never descends below the leaves.
+cbq_status validate_heights(const uint32_t* nodes, uint64_t node_count, const cbq_subdag subdags[8]);
+
 }  // namespace cbq
 
 // The opaque DAG handle.
@@ -26,6 +30,8 @@ struct cbq_dag {
     cbq_subdag subdags[8];
     int32_t max_height = 0;        // max SubDAG height (stack depth)
     int device = 0;
+    bool flat_ok = false;          // float positions exact (coordinates within +-2^24)
+    cbq_launch_config cfg{CBQ_KERNEL_AUTO, 0, 0, 0};
 
     // Staging for cbq_intersect_host.
     std::mutex staging_lock;

@@ -126,6 +126,30 @@ cbq_status cbq_dag_create(const uint32_t* host_nodes, uint64_t node_count, uint3
 cbq_status cbq_dag_destroy(cbq_dag* dag);
 cbq_status cbq_dag_get_info(const cbq_dag* dag, cbq_dag_info* info);
 
+/* Kernel selection and launch shape (chosen by the autotuner; 0 = default).
+ *   CBQ_KERNEL_FLAT    one ray per thread, the ESVO loops flattened into one
+ *                      per-lane state machine (lanes reconverge every step);
+ *                      used when the DAG's coordinates lie within +-2^24
+ *   CBQ_KERNEL_NESTED  one ray per thread, the reference's nested loops as
+ *                      written (any coordinates)
+ * For cbq_intersect_persistent, `refill_min` (flat) is the number of idle lanes
+ * at which a warp takes new rays and `chunk` (nested) the rays per warp grab. */
+typedef enum cbq_kernel {
+    CBQ_KERNEL_AUTO = 0,
+    CBQ_KERNEL_NESTED = 1,
+    CBQ_KERNEL_FLAT = 2
+} cbq_kernel;
+
+typedef struct cbq_launch_config {
+    int32_t kernel;           /* cbq_kernel */
+    int32_t block;            /* threads per block (multiple of 32, <= 256), 0 = default */
+    uint32_t chunk;           /* nested persistent: rays per warp grab, 0 = default */
+    uint32_t refill_min;      /* flat persistent: idle lanes that trigger a refill, 0 = default */
+} cbq_launch_config;
+
+cbq_status cbq_dag_set_launch_config(cbq_dag* dag, const cbq_launch_config* cfg);
+cbq_status cbq_dag_get_launch_config(const cbq_dag* dag, cbq_launch_config* cfg);
+
 /* Sets a persisting-L2 access-policy window over the node store on `stream`
  * (fraction of the device's persisting-L2 limit to reserve, 0 disables). */
 cbq_status cbq_dag_set_l2_persistence(const cbq_dag* dag, cbq_stream_t stream, float fraction);
@@ -144,10 +168,11 @@ cbq_status cbq_intersect_host(const cbq_dag* dag, const float* host_origin_tmax,
                               const float* host_direction, uint64_t n, const cbq_query* query,
                               const cbq_hits* host_hits);
 
-/* Persistent form: a grid sized to the device's SMs whose warps pull chunks of
- * `chunk` rays from an atomic work counter.  `work_counter` is caller-owned
- * device scratch (one uint64, zeroed by this call on `stream`).  chunk = 0
- * selects the tuned default. */
+/* Persistent form: a grid sized to the device's SMs whose warps pull rays from
+ * an atomic work counter.  `work_counter` is caller-owned device scratch (one
+ * uint64, zeroed by this call on `stream`).  With the flat kernel a warp takes
+ * new rays whenever `chunk` (<= 32) of its lanes are idle; with the nested one
+ * it takes `chunk` rays at a time.  chunk = 0 selects the tuned default. */
 cbq_status cbq_intersect_persistent(const cbq_dag* dag, const cbq_rays* rays, uint64_t n,
                                     const cbq_query* query, const cbq_hits* hits,
                                     uint64_t* work_counter, uint32_t chunk, cbq_stream_t stream);

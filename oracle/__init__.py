@@ -75,6 +75,35 @@ def _subdag_array(subdags) -> "ctypes.Array":
     return arr
 
 
+def undefined_stack_rays(orc: "Oracle", nodes, subdags, origin_tmax, direction, **kw) -> np.ndarray:
+    """Indices of rays whose result depends on never-written descent-stack slots
+    (uninitialised in the reference, so its result there is undefined)."""
+    a = orc.intersect(nodes, subdags, origin_tmax, direction, **kw)
+    b = orc.intersect(nodes, subdags, origin_tmax, direction, unwritten_slot_is_start_node=True, **kw)
+    diff = np.zeros(a["hit"].shape[0], bool)
+    for k in ("hit", "material", "status", "voxel", "normal"):
+        diff |= (a[k] != b[k]).reshape(diff.size, -1).any(axis=1)
+    return np.nonzero(diff)[0]
+
+
+def same_bits_nan_equal(a, b) -> bool:
+    """Bit equality, except that every NaN equals every NaN: NaN payloads differ
+    between x86, Arm and the GPU even for the reference itself."""
+    a = np.ascontiguousarray(a)
+    b = np.ascontiguousarray(b)
+    if a.shape != b.shape:
+        return False
+    if a.dtype.kind == "f" and b.dtype.kind == "f":
+        if a.dtype != b.dtype:
+            return False
+        na, nb = np.isnan(a), np.isnan(b)
+        if not np.array_equal(na, nb):
+            return False
+        a = np.where(na, 0, a)
+        b = np.where(nb, 0, b)
+    return np.array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
 def _alloc(n: int) -> dict:
     return {"hit": np.zeros(n, np.uint8), "distance": np.zeros(n, np.float32), "material": np.zeros(n, np.uint32),
             "position": np.zeros((n, 3), np.float32), "normal": np.zeros((n, 3), np.float32),
@@ -91,6 +120,7 @@ class Oracle:
         lib.orc_find_subdags.argtypes = [_P, _U64, _U32, ctypes.POINTER(OrcSubdag)]
         lib.orc_intersect_batch.argtypes = [_P, _U64, ctypes.POINTER(OrcSubdag), _P, _P, _U64, ctypes.c_int,
                                             ctypes.c_float, ctypes.c_int, ctypes.POINTER(OrcHits), ctypes.c_int]
+        lib.orc_intersect_batch_ex.argtypes = lib.orc_intersect_batch.argtypes + [ctypes.c_int]
         lib.orc_count_fetches.argtypes = [_P, _U64, ctypes.POINTER(OrcSubdag), _P, _P, _U64, ctypes.c_int,
                                           ctypes.c_float, _P, ctypes.c_int]
         lib.orc_trace_fp64_batch.argtypes = [_P, _U64, ctypes.POINTER(OrcSubdag), _P, _P, _U64, _P, _P, _P,
@@ -106,7 +136,7 @@ class Oracle:
         return [(tuple(s.lower), s.height, s.node) for s in out]
 
     def intersect(self, nodes, subdags, origin_tmax, direction, compute_surface=True, max_footprint=-1.0,
-                  use_tmax=False, threads=0) -> dict:
+                  use_tmax=False, threads=0, unwritten_slot_is_start_node=False) -> dict:
         nodes = np.ascontiguousarray(nodes, dtype=np.uint32)
         o = np.ascontiguousarray(origin_tmax, dtype=np.float32).reshape(-1, 4)
         d = np.ascontiguousarray(direction, dtype=np.float32).reshape(-1, 4)
@@ -114,9 +144,9 @@ class Oracle:
         out = _alloc(n)
         hits = OrcHits(*[_ptr(out[k]) for k in ("hit", "distance", "material", "position", "normal", "voxel",
                                                 "status")])
-        rc = self.lib.orc_intersect_batch(_ptr(nodes), nodes.size // 8, _subdag_array(subdags), _ptr(o), _ptr(d), n,
-                                          1 if compute_surface else 0, max_footprint, 1 if use_tmax else 0,
-                                          ctypes.byref(hits), threads)
+        rc = self.lib.orc_intersect_batch_ex(_ptr(nodes), nodes.size // 8, _subdag_array(subdags), _ptr(o), _ptr(d),
+                                             n, 1 if compute_surface else 0, max_footprint, 1 if use_tmax else 0,
+                                             ctypes.byref(hits), threads, 1 if unwritten_slot_is_start_node else 0)
         if rc:
             raise RuntimeError(f"orc_intersect_batch failed ({rc})")
         return out

@@ -117,6 +117,7 @@ typedef struct ray_ctx {
     float max_footprint;
     uint32_t fetches;
     uint32_t status;
+    int fill_start;   /* never-written stack slots read as the walk's start node instead of 0 */
 } ray_ctx;
 
 typedef struct esvo_out {
@@ -188,7 +189,7 @@ static esvo_out esvo(ray_ctx* r, uint32_t node, int32_t px, int32_t py, int32_t 
     int32_t cz = wadd(pz, (cid & 4u) ? cns : 0);
     float last_exit = exit_;
     uint32_t stack[33];
-    memset(stack, 0, sizeof(stack));
+    for (int q = 0; q < 33; q++) stack[q] = r->fill_start ? node : 0u;
 
     do {
         const float c1x = ((float)wadd(cx, cns) - r->o[0]) * r->inv[0];
@@ -256,10 +257,12 @@ static esvo_out esvo(ray_ctx* r, uint32_t node, int32_t px, int32_t py, int32_t 
 
 /* intersectVolume (raytracing.cpp:407-478). */
 static void intersect_one(const uint32_t* nodes, const orc_subdag sd[8], const float* o4, const float* d4,
-                          int cs, float mf, int use_tmax, const orc_hits* out, uint64_t i, uint32_t* fetches)
+                          int cs, float mf, int use_tmax, const orc_hits* out, uint64_t i, uint32_t* fetches,
+                          int fill_start)
 {
     ray_ctx r;
     r.nodes = nodes;
+    r.fill_start = fill_start;
     r.compute_surface = cs;
     r.max_footprint = mf;
     r.fetches = 0;
@@ -433,6 +436,7 @@ typedef struct job {
     uint8_t* hit;
     double* dist64;
     uint32_t* mat;
+    int fill_start;
     uint64_t next; /* atomic cursor */
 } job;
 
@@ -450,7 +454,7 @@ static void* worker(void* arg)
                 trace64_one(j->nodes, j->sd, j->o4 + 4 * i, j->d4 + 4 * i, j->hit, j->dist64, j->mat, i);
             else
                 intersect_one(j->nodes, j->sd, j->o4 + 4 * i, j->d4 + 4 * i, j->cs, j->mf, j->use_tmax,
-                              j->kind == 0 ? j->out : NULL, i, j->fetches);
+                              j->kind == 0 ? j->out : NULL, i, j->fetches, j->fill_start);
         }
     }
     return NULL;
@@ -490,9 +494,10 @@ static int check_nodes(const uint32_t* nodes, uint64_t node_count, const orc_sub
     return 0;
 }
 
-int orc_intersect_batch(const uint32_t* nodes, uint64_t node_count, const orc_subdag subdags[8],
-                        const float* orig4, const float* dir4, uint64_t n, int compute_surface,
-                        float max_footprint, int use_tmax, const orc_hits* out, int nthreads)
+int orc_intersect_batch_ex(const uint32_t* nodes, uint64_t node_count, const orc_subdag subdags[8],
+                           const float* orig4, const float* dir4, uint64_t n, int compute_surface,
+                           float max_footprint, int use_tmax, const orc_hits* out, int nthreads,
+                           int unwritten_slot_is_start_node)
 {
     int rc = check_nodes(nodes, node_count, subdags);
     if (rc) return rc;
@@ -500,7 +505,16 @@ int orc_intersect_batch(const uint32_t* nodes, uint64_t node_count, const orc_su
     memset(&j, 0, sizeof(j));
     j.kind = 0; j.nodes = nodes; j.sd = subdags; j.o4 = orig4; j.d4 = dir4; j.n = n;
     j.cs = compute_surface; j.mf = max_footprint; j.use_tmax = use_tmax; j.out = out;
+    j.fill_start = unwritten_slot_is_start_node;
     return run_job(&j, nthreads);
+}
+
+int orc_intersect_batch(const uint32_t* nodes, uint64_t node_count, const orc_subdag subdags[8],
+                        const float* orig4, const float* dir4, uint64_t n, int compute_surface,
+                        float max_footprint, int use_tmax, const orc_hits* out, int nthreads)
+{
+    return orc_intersect_batch_ex(nodes, node_count, subdags, orig4, dir4, n, compute_surface, max_footprint,
+                                  use_tmax, out, nthreads, 0);
 }
 
 int orc_count_fetches(const uint32_t* nodes, uint64_t node_count, const orc_subdag subdags[8],

@@ -70,6 +70,17 @@ int orc_intersect_batch(const uint32_t* nodes, uint64_t node_count,
                         int compute_surface, float max_footprint, int use_tmax,
                         const orc_hits* out, int nthreads);
 
+/* As orc_intersect_batch; with unwritten_slot_is_start_node != 0 a descent-
+ * stack slot that was never written reads as the walk's start node instead of
+ * node 0.  The reference leaves those slots uninitialised, so a ray whose
+ * result changes between the two settings depends on undefined values there;
+ * tests use this to identify and list such rays. */
+int orc_intersect_batch_ex(const uint32_t* nodes, uint64_t node_count,
+                           const orc_subdag subdags[8],
+                           const float* orig4, const float* dir4, uint64_t n,
+                           int compute_surface, float max_footprint, int use_tmax,
+                           const orc_hits* out, int nthreads, int unwritten_slot_is_start_node);
+
 /* Counts the node fetches (dependent child loads) each ray performs. */
 int orc_count_fetches(const uint32_t* nodes, uint64_t node_count,
                       const orc_subdag subdags[8],

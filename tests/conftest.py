@@ -51,5 +51,28 @@ def digests():
     return json.loads((GOLDEN / "digests.json").read_text())
 
 
+def relocate(nodes, root, edge_log2, origin):
+    """Moves a scene built at the origin (box [0, 2^edge_log2)^3) so that its
+    box starts at `origin` (multiples of 2^edge_log2): re-links the chain of
+    single-child nodes between the scene's top node and the root."""
+    import numpy as np
+    n = nodes.reshape(-1, 8)
+    node = int(n[root][7])                      # height 31: unsigned bit 31 set on every axis
+    for _ in range(31 - edge_log2):
+        node = int(n[node][0])                  # heights 30 .. edge_log2: bits clear
+    extra = []
+    count = n.shape[0]
+    u = [(int(o) + (1 << 31)) & 0xFFFFFFFF for o in origin]
+    for hh in range(edge_log2 + 1, 33):
+        b = hh - 1
+        cid = ((u[0] >> b) & 1) | (((u[1] >> b) & 1) << 1) | (((u[2] >> b) & 1) << 2)
+        row = [0] * 8
+        row[cid] = node
+        extra.append(row)
+        node = count + len(extra) - 1
+    out = np.concatenate([nodes.reshape(-1), np.array(extra, dtype=np.uint32).reshape(-1)])
+    return out, node
+
+
 def subdags_of(fx):
     return [((int(r[0]), int(r[1]), int(r[2])), int(r[3]), int(r[4])) for r in fx["subdags"]]

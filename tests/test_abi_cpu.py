@@ -65,6 +65,14 @@ def test_validate_rejects_malformed():
         cbq.validate(nodes, nodes.size // 8)
     with pytest.raises(cbq.CbqError):
         cbq.validate(nodes[: 8 * 100], 0)
+    # A cycle (a node that is its own child) would let a traversal descend
+    # below the leaves; it is rejected before any upload.
+    sd = cbq.find_subdags(nodes, root)[7]
+    bad = nodes.copy()
+    bad[8 * sd.node_index + 3] = sd.node_index
+    with pytest.raises(cbq.CbqError) as e:
+        cbq.validate(bad, root)
+    assert e.value.status == 2
 
 
 def test_find_subdags_matches_golden(golden):
@@ -125,6 +133,21 @@ def test_reorder_bfs_keeps_the_graph(orc):
     b = orc.intersect(n2, orc.find_subdags(n2, r2), o, d)
     for k in ("hit", "distance", "material", "position", "normal", "voxel"):
         assert np.array_equal(a[k], b[k])
+
+
+def test_relocated_scene_voxels_and_subdags():
+    from conftest import relocate
+    nodes, root = W.SceneSpec(cbq.SCENE_SPHERES, 6, 21, 10).build()
+    origin = (1 << 30, -(1 << 26), 3 << 20)
+    n2, r2 = relocate(nodes, root, 6, origin)
+    cbq.validate(n2, r2)
+    rng = np.random.default_rng(3)
+    for x, y, z in rng.integers(0, 64, (300, 3)):
+        a = cbq.dag_voxel(nodes, root, int(x), int(y), int(z))
+        b = cbq.dag_voxel(n2, r2, int(x) + origin[0], int(y) + origin[1], int(z) + origin[2])
+        assert a == b
+    sd = [s for s in cbq.find_subdags(n2, r2) if s.node_index]
+    assert len(sd) == 1 and tuple(sd[0].lower_bound) == origin
 
 
 def test_bounce_rays_are_unit_and_in_hemisphere():
