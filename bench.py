@@ -52,12 +52,15 @@ def parse_args():
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     p.add_argument("--workload", choices=["terrain-4096", "spheres-256"], default="terrain-4096")
     p.add_argument("--kernel", choices=["auto", "flat", "nested"], default="auto")
-    p.add_argument("--persistent", action="store_true", help="persistent grid pulling rays from a work counter")
+    p.add_argument("--form", choices=["persistent", "plain"], default="persistent",
+                   help="persistent grid pulling rays from a work counter, or one thread per ray")
     p.add_argument("--block", type=int, default=0)
     p.add_argument("--chunk", type=int, default=0, help="persistent: refill threshold (flat) / grab size (nested)")
     p.add_argument("--e2e-steps", type=int, default=5)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    return p.parse_args()
+    args = p.parse_args()
+    args.persistent = args.form == "persistent"
+    return args
 
 
 # ------------------------------------------------------------------ workload

@@ -20,7 +20,7 @@ cbq_status launch_flat(const cbq_dag* dag, const dev::DagParams& dp, const dev::
 
 namespace {
 
-constexpr int kFlatBlockDefault = 128;
+constexpr int kFlatBlockDefault = 64;  // GB300 sweep, terrain-4096: 64 >= 128 > 256 threads
 constexpr uint32_t kRefillDefault = 8;
 
 bool use_flat(const cbq_dag* dag)
@@ -211,9 +211,10 @@ cbq_status cbq_intersect(const cbq_dag* dag, const cbq_rays* rays, uint64_t n, c
                          const cbq_hits* hits, cbq_stream_t stream)
 {
     if (!dag || !hits) return CBQ_ERR_INVALID_ARGUMENT;
+    if (!rays) return CBQ_ERR_INVALID_ARGUMENT;
+    if (n == 0) return CBQ_OK;  // an empty batch may carry NULL buffers
     cbq_status st = check_rays(rays);
     if (st != CBQ_OK) return st;
-    if (n == 0) return CBQ_OK;
     if (use_flat(dag))
         return launch_flat(dag, make_dag_params(dag), make_query(query), make_hits(hits),
                            (const float4*)rays->origin_tmax, (const float4*)rays->direction, n, nullptr, false,
@@ -251,9 +252,10 @@ cbq_status cbq_count_fetches(const cbq_dag* dag, const cbq_rays* rays, uint64_t 
                              uint32_t* fetches, cbq_stream_t stream)
 {
     if (!dag || !fetches) return CBQ_ERR_INVALID_ARGUMENT;
+    if (!rays) return CBQ_ERR_INVALID_ARGUMENT;
+    if (n == 0) return CBQ_OK;  // an empty batch may carry NULL buffers
     cbq_status st = check_rays(rays);
     if (st != CBQ_OK) return st;
-    if (n == 0) return CBQ_OK;
     dev::HitsOut none;
     std::memset(&none, 0, sizeof(none));
     if (use_flat(dag))
@@ -272,9 +274,10 @@ cbq_status cbq_intersect_persistent(const cbq_dag* dag, const cbq_rays* rays, ui
                                     cbq_stream_t stream)
 {
     if (!dag || !hits || !work_counter) return CBQ_ERR_INVALID_ARGUMENT;
+    if (!rays) return CBQ_ERR_INVALID_ARGUMENT;
+    if (n == 0) return CBQ_OK;  // an empty batch may carry NULL buffers
     cbq_status st = check_rays(rays);
     if (st != CBQ_OK) return st;
-    if (n == 0) return CBQ_OK;
     if (use_flat(dag)) {
         const uint32_t refill = chunk ? std::min<uint32_t>(chunk, 32u)
                                       : (dag->cfg.refill_min ? dag->cfg.refill_min : kRefillDefault);
@@ -330,6 +333,9 @@ cbq_status cbq_intersect_host(const cbq_dag* cdag, const float* host_origin_tmax
     dh.material = (uint32_t*)p; p += n * 4;
     dh.hit = (uint8_t*)p; p += n;
     dh.status = (uint8_t*)p;
+    p += n;
+    // The persistent kernel's work counter: 8-byte aligned after the hit fields.
+    uint64_t* d_counter = (uint64_t*)(((uintptr_t)p + 7u) & ~(uintptr_t)7u);
     cudaStream_t s = 0;
     if (cudaMemcpyAsync(d_o, host_origin_tmax, n * 16, cudaMemcpyHostToDevice, s) != cudaSuccess) return CBQ_ERR_CUDA;
     if (cudaMemcpyAsync(d_d, host_direction, n * 16, cudaMemcpyHostToDevice, s) != cudaSuccess) return CBQ_ERR_CUDA;
@@ -342,7 +348,8 @@ cbq_status cbq_intersect_host(const cbq_dag* cdag, const float* host_origin_tmax
     if (!host_hits->voxel) launch.voxel = nullptr;
     if (!host_hits->status) launch.status = nullptr;
     cbq_rays rays{d_o, d_d};
-    cbq_status st = cbq_intersect(dag, &rays, n, query, &launch, (cbq_stream_t)s);
+    // Persistent form: its counter is private to this call (staging lock held).
+    cbq_status st = cbq_intersect_persistent(dag, &rays, n, query, &launch, d_counter, 0u, (cbq_stream_t)s);
     if (st != CBQ_OK) return st;
     struct Copy { void* dst; const void* src; size_t bytes; };
     const Copy copies[] = {
