@@ -327,8 +327,8 @@ public:
         edge_ = 1 << edge_log2;
         hmin_ = edge_ / 8;
         hmax_ = edge_ / 2;
-        band_log2_ = edge_log2 - 5;
-        cave_log2_ = edge_log2 - 5;
+        band_log2_ = std::max(0, edge_log2 - 5);
+        cave_log2_ = std::max(0, edge_log2 - 5);
         base_log2_ = edge_log2 - 2;
         make_heights();
         make_cave_lattice();
@@ -378,7 +378,7 @@ private:
         std::vector<std::vector<double>> lat(octaves);
         std::vector<int> per(octaves), cells(octaves);
         for (int o = 0; o < octaves; o++) {
-            per[o] = 1 << (base_log2_ - o);
+            per[o] = 1 << std::max(0, base_log2_ - o);  // octaves finer than a voxel repeat the voxel
             cells[o] = edge_ / per[o] + 1;
             lat[o].resize((size_t)cells[o] * cells[o]);
             for (int j = 0; j < cells[o]; j++)
