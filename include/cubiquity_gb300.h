@@ -168,6 +168,28 @@ cbq_status cbq_intersect_host(const cbq_dag* dag, const float* host_origin_tmax,
                               const float* host_direction, uint64_t n, const cbq_query* query,
                               const cbq_hits* host_hits);
 
+/* No counterpart in the reference.  As cbq_intersect_host, but without any
+ * device allocation, for callers that must not call cudaMalloc: a render or
+ * physics thread with a frame deadline (cudaMalloc can synchronise the device
+ * and stall every stream), or a host application whose own allocator owns all
+ * device memory.  Rays and hits are staged, and the persistent kernel's work
+ * counter kept, in one fixed array compiled into the library
+ * (CBQ_NOALLOC_MAX_RAYS * 78 bytes + 256, about 5 MB, held on every device that
+ * loads the library until the process exits).
+ *   - n > CBQ_NOALLOC_MAX_RAYS returns CBQ_ERR_CAPACITY; nothing is launched.
+ *   - The current device must be the DAG's device.  The first call on a device
+ *     looks up the array's device address (cudaGetSymbolAddress); make that
+ *     first call before any stream capture.
+ *   - Every call on a device shares the array and leaves its contents behind;
+ *     each call rewrites what it reads (rays, hits) and zeroes the counter.
+ *     Calls that overlap on the GPU (for instance from several host threads)
+ *     race on the array: callers must serialise them.
+ *   - Synchronous, like cbq_intersect_host. */
+#define CBQ_NOALLOC_MAX_RAYS 65536u
+cbq_status cbq_intersect_host_noalloc(const cbq_dag* dag, const float* host_origin_tmax,
+                                      const float* host_direction, uint64_t n, const cbq_query* query,
+                                      const cbq_hits* host_hits);
+
 /* Persistent form: a grid sized to the device's SMs whose warps pull rays from
  * an atomic work counter.  `work_counter` is caller-owned device scratch (one
  * uint64, zeroed by this call on `stream`).  With the flat kernel a warp takes
