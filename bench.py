@@ -50,7 +50,7 @@ def parse_args():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    p.add_argument("--workload", choices=["terrain-4096", "spheres-256"], default="terrain-4096")
+    p.add_argument("--workload", choices=["terrain-4096", "spheres-256", "batch-64"], default="terrain-4096")
     p.add_argument("--kernel", choices=["auto", "flat", "nested"], default="auto")
     p.add_argument("--form", choices=["persistent", "plain"], default="persistent",
                    help="persistent grid pulling rays from a work counter, or one thread per ray")
@@ -416,11 +416,186 @@ def run_gpu(args, world, rank, local):
     dag.destroy()
 
 
+def batch_jobs():
+    """The 64-volume batching workload as [(nodes, root, origin_tmax, direction)]."""
+    from cubiquity_gb300 import workloads as W
+
+    jobs = []
+    for v in W.batch_volumes():
+        nodes, root = v.scene.build()
+        o, d = v.make_rays()
+        jobs.append((nodes, root, o, d))
+    return jobs
+
+
+def run_reference_batch(args, world, rank):
+    if rank != 0:
+        return
+    import oracle
+
+    jobs = batch_jobs()
+    rays = sum(j[2].shape[0] for j in jobs)
+    use_ref = oracle.reference_available()
+    if use_ref:
+        ref = oracle.Reference()
+        vols = [ref.volume_from_nodes(n, r) for n, r, _, _ in jobs]
+        sds = [v.find_subdags() for v in vols]
+    else:
+        orc = oracle.Oracle()
+        sds = [orc.find_subdags(n, r) for n, r, _, _ in jobs]
+
+    def step():
+        t0 = time.perf_counter()
+        for k, (n, r, o, d) in enumerate(jobs):
+            if use_ref:
+                vols[k].intersect(sds[k], o, d, True, -1.0)
+            else:
+                orc.intersect(n, sds[k], o, d, True, -1.0)
+        return time.perf_counter() - t0
+
+    for _ in range(args.warmup):
+        step()
+    total = sum(step() for _ in range(args.steps))
+    value = rays * args.steps / total / 1e6
+    cores = host_cores()
+    kind = "reference" if use_ref else "port"
+    print(json.dumps({
+        "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (64 seeded volumes, generated rays)",
+        "impl": "reference", "config": {"workload": "batch-64", "rays_per_step": rays, "volumes": len(jobs)},
+        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": cores, "kind": kind,
+                         "sample": f"all 64 volumes ({rays} rays) per step on {cores} host threads"},
+        "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}), flush=True)
+
+
+def run_gpu_batch(args, world, rank, local):
+    """configs[2]: many volumes of uneven size in one persistent, graph-captured,
+    autotuned launch, against the plain kernel launched once per volume."""
+    import torch
+    import cubiquity_gb300 as cbq
+
+    torch.cuda.set_device(local)
+    host_jobs = batch_jobs()
+    dags = [cbq.Dag(n, r) for n, r, _, _ in host_jobs]
+    dev = [(torch.from_numpy(o).cuda(), torch.from_numpy(d).cuda()) for _, _, o, d in host_jobs]
+    rays_per_step = sum(o.shape[0] for o, _ in dev)
+    stream = torch.cuda.current_stream()
+    plain_out = [cbq.alloc_hits(o.shape[0]) for o, _ in dev]
+    batch = cbq.Batch([(g, o, d) for g, (o, d) in zip(dags, dev)])
+    tuned = batch.autotune(3, stream=stream)
+
+    def plain_step():
+        for g, (o, d), out in zip(dags, dev, plain_out):
+            cbq.intersect_volume(g, o, d, out=out, stream=stream)
+
+    def batched_step():
+        batch.launch(stream=stream)
+
+    def timed(fn, steps):
+        for _ in range(max(3, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        barrier(world)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+        return max_over_ranks(world, e0.elapsed_time(e1))
+
+    plain_ms = timed(plain_step, args.steps)
+    clocks = ClockSampler(local)
+    clocks.start()
+    batched_ms = timed(batched_step, args.steps)
+    clk = clocks.stop()
+    # Same answers from both forms.
+    for out_b, out_p in zip(batch.outputs, plain_out):
+        for k in ("hit", "material", "voxel", "distance", "status"):
+            if not torch.equal(out_b[k], out_p[k]):
+                raise SystemExit(f"batched and plain results differ in {k}")
+    value = rays_per_step * args.steps * world / (batched_ms * 1e-3) / 1e6
+    plain_value = rays_per_step * args.steps * world / (plain_ms * 1e-3) / 1e6
+
+    # Roofline of the batched launch.
+    fetches = sum(cbq.count_fetches(g, o, d).double().sum().item() for g, (o, d) in zip(dags, dev))
+    peak, peak_kind = measured_peaks()
+    step_s = batched_ms / args.steps * 1e-3
+    alg_bytes = rays_per_step * (RAY_BYTES + HIT_BYTES) + fetches * SECTOR
+    achieved = alg_bytes / step_s / 1e9
+    l2_stream, l2_rand = cbq.measure_l2(64 << 20, 20)
+
+    # End to end: pinned host rays in, one batched launch, hits out.
+    pinned_in = [(torch.from_numpy(o).pin_memory(), torch.from_numpy(d).pin_memory()) for _, _, o, d in host_jobs]
+    pinned_out = [{k: torch.empty(v.shape, dtype=v.dtype).pin_memory() for k, v in out.items()}
+                  for out in batch.outputs]
+
+    def e2e_step():
+        for (po, pd), (o, d) in zip(pinned_in, dev):
+            o.copy_(po, non_blocking=True)
+            d.copy_(pd, non_blocking=True)
+        batch.launch(stream=stream)
+        for out, host in zip(batch.outputs, pinned_out):
+            for k, v in out.items():
+                host[k].copy_(v, non_blocking=True)
+        torch.cuda.synchronize()
+
+    e2e_step()
+    t = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    e2e_value = rays_per_step * args.e2e_steps * world / max_over_ranks(world, time.perf_counter() - t) / 1e6
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import oracle
+        orc = oracle.Oracle()
+        t0 = time.perf_counter()
+        for n, r, o, d in host_jobs:
+            orc.intersect(n, orc.find_subdags(n, r), o, d)
+        dt = time.perf_counter() - t0
+        cpu = {"value": rays_per_step / dt / 1e6, "unit": "Mrays/s", "cores": host_cores(), "kind": "port",
+               "sample": f"one pass over all 64 volumes ({rays_per_step} rays), {host_cores()} host threads"}
+    line = {
+        "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": batched_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (64 seeded sphere/terrain volumes, edges 2^7..2^11, generated rays)",
+        "config": {"workload": "batch-64", "volumes": len(dags), "rays_per_step": rays_per_step,
+                   "dag_bytes": int(sum(g.bytes for g in dags)), "batch_config": tuned,
+                   "form": "one persistent launch replayed from a CUDA graph",
+                   "l2": "inputs larger than L2 (rays + hits %.0f MB per step)" % (rays_per_step * 78 / 1e6)},
+        "plain": {"value": plain_value, "unit": "Mrays/s", "ms_per_step": plain_ms / args.steps,
+                  "form": "cbq_intersect once per volume (64 launches per step)"},
+        "batched_over_plain": value / plain_value,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": f"{peak_kind} hbm_gbs", "kernel": "cbq_k_flat_batch", "traffic": None,
+                     "fetches_per_ray": fetches / rays_per_step,
+                     "l2": {"stream_peak_gbs": l2_stream, "frac_stream": achieved / l2_stream,
+                            "sector_rate_gsps": fetches / step_s / 1e9, "random_sector_peak_gsps": l2_rand}},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": rays_per_step * RAY_BYTES,
+                "d2h_bytes_per_step": rays_per_step * HIT_BYTES},
+        "gpu_launches": args.steps,
+        "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
-        run_reference(args, world, rank)
+        if args.workload == "batch-64":
+            run_reference_batch(args, world, rank)
+        else:
+            run_reference(args, world, rank)
+    elif args.workload == "batch-64":
+        run_gpu_batch(args, world, rank, local)
     else:
         run_gpu(args, world, rank, local)
     if world > 1:

@@ -135,6 +135,30 @@ _sig("cbq_gen_pinhole_rays", [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ct
                               _I32, _I32, _P, _P])
 _sig("cbq_gen_bounce_rays", [_P, _P, _U64, _U64, _U64, _P, _P])
 _sig("cbq_measure_l2", [_U64, ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)])
+_sig("cbq_gen_sphere_rays", [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), _U64, _U64, _P, _P])
+
+
+class _Job(ctypes.Structure):
+    _fields_ = [("dag", ctypes.c_void_p), ("rays", _Rays), ("ray_count", ctypes.c_uint64), ("hits", _Hits)]
+
+
+_sig("cbq_batch_create", [ctypes.POINTER(_Job), ctypes.c_int32, ctypes.POINTER(_Query), ctypes.POINTER(_P)])
+_sig("cbq_batch_set_config", [_P, ctypes.c_int32, _U32])
+_sig("cbq_batch_get_config", [_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(_U32), ctypes.POINTER(_U64)])
+_sig("cbq_batch_autotune", [_P, _P, ctypes.c_int32])
+_sig("cbq_batch_launch", [_P, _P])
+_sig("cbq_batch_launch_direct", [_P, _P])
+_sig("cbq_batch_destroy", [_P])
+_sig("cbq_intersect_batch", [ctypes.POINTER(_Job), ctypes.c_int32, ctypes.POINTER(_Query), _P])
+
+
+def sphere_rays(lo, hi, n: int, seed: int) -> tuple[np.ndarray, np.ndarray]:
+    """Origins uniform in the box [lo, hi], directions uniform on the sphere."""
+    o = np.empty((n, 4), dtype=np.float32)
+    d = np.empty((n, 4), dtype=np.float32)
+    _check(_lib.cbq_gen_sphere_rays((ctypes.c_double * 3)(*lo), (ctypes.c_double * 3)(*hi), n, seed, _np_ptr(o),
+                                    _np_ptr(d)), "cbq_gen_sphere_rays")
+    return o, d
 
 
 def _check(status: int, what: str) -> None:
@@ -443,3 +467,65 @@ def intersect_volume_host(dag: Dag, origin_tmax: np.ndarray, direction: np.ndarr
     _check(_lib.cbq_intersect_host(dag.handle, _np_ptr(o), _np_ptr(d), n, ctypes.byref(q), ctypes.byref(hits)),
            "cbq_intersect_host")
     return out
+
+
+# ------------------------------------------------------------ batched form
+
+class Batch:
+    """Many volumes with their own ray batches in one persistent, graph-captured
+    launch (cbq_batch).  `jobs` is a list of (Dag, origin_tmax, direction) with
+    CUDA tensors; outputs are allocated per job (``self.outputs[i]``)."""
+
+    def __init__(self, jobs, compute_surface_properties: bool = True,
+                 max_footprint: float = MAX_FOOTPRINT_DISABLED, use_tmax: bool = False, outputs=None):
+        self.jobs = list(jobs)
+        self.outputs = outputs if outputs is not None else [alloc_hits(o.shape[0], o.device) for _, o, _ in self.jobs]
+        arr = (_Job * max(1, len(self.jobs)))()
+        for i, (dag, o, d) in enumerate(self.jobs):
+            _check_rays_tensor(o)
+            _check_rays_tensor(d, o.shape[0])
+            arr[i].dag = dag.handle
+            arr[i].rays = _Rays(o.data_ptr(), d.data_ptr())
+            arr[i].ray_count = o.shape[0]
+            arr[i].hits = _hits_struct(self.outputs[i])
+        self._q = Query(compute_surface_properties, max_footprint, use_tmax).c()
+        h = _P()
+        _check(_lib.cbq_batch_create(arr, len(self.jobs), ctypes.byref(self._q), ctypes.byref(h)), "cbq_batch_create")
+        self._h = h
+
+    @property
+    def total_rays(self) -> int:
+        return self.config()["total_rays"]
+
+    def config(self) -> dict:
+        b = ctypes.c_int32()
+        r = _U32()
+        t = _U64()
+        _check(_lib.cbq_batch_get_config(self._h, ctypes.byref(b), ctypes.byref(r), ctypes.byref(t)),
+               "cbq_batch_get_config")
+        return {"block": b.value, "refill_min": r.value, "total_rays": t.value}
+
+    def set_config(self, block: int = 0, refill_min: int = 0) -> None:
+        _check(_lib.cbq_batch_set_config(self._h, block, refill_min), "cbq_batch_set_config")
+
+    def autotune(self, repetitions: int = 3, stream=None) -> dict:
+        _check(_lib.cbq_batch_autotune(self._h, _stream_ptr(stream), repetitions), "cbq_batch_autotune")
+        return self.config()
+
+    def launch(self, stream=None) -> None:
+        """Replays the captured CUDA graph (captured on first use)."""
+        _check(_lib.cbq_batch_launch(self._h, _stream_ptr(stream)), "cbq_batch_launch")
+
+    def launch_direct(self, stream=None) -> None:
+        _check(_lib.cbq_batch_launch_direct(self._h, _stream_ptr(stream)), "cbq_batch_launch_direct")
+
+    def destroy(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            _lib.cbq_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass

@@ -1,0 +1,354 @@
+// Batched traversal: many volumes, each with its own ray batch, in one
+// persistent launch, captured in a CUDA graph and replayed (cbq_batch_*).
+//
+// A job table in device memory holds, per job, the node store, the SubDAGs, the
+// ray and hit arrays and the job's first global ray index.  Persistent warps
+// take global ray indices from one atomic counter (warp-aggregated refill of
+// idle lanes, as in the single-volume persistent kernel); a lane finds its job
+// by binary search over the prefix offsets, held in shared memory.
+#include "cbq_flat.cuh"
+#include "cbq_internal.hpp"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <vector>
+
+namespace cbq {
+namespace dev {
+
+struct JobDesc {
+    const uint32_t* nodes;
+    const float4* orig;
+    const float4* dir;
+    HitsOut out;
+    uint64_t first;   // global index of the job's first ray
+    uint64_t count;
+    SubDag sd[8];
+};
+
+struct BatchSrc {
+    const JobDesc* __restrict__ jobs;
+    QueryParams q;
+
+    __device__ __forceinline__ const uint32_t* nodes(const Lane& L) const { return L.nodes; }
+    __device__ __forceinline__ const SubDag& subdag(const Lane& L, uint32_t k) const { return jobs[L.job].sd[k]; }
+    __device__ __forceinline__ float4 ray_origin(const Lane& L, uint64_t i) const { return __ldg(jobs[L.job].orig + i); }
+    __device__ __forceinline__ float4 ray_direction(const Lane& L, uint64_t i) const { return __ldg(jobs[L.job].dir + i); }
+    __device__ __forceinline__ void write(const Lane& L, const RayResult& r) const
+    {
+        write_result(jobs[L.job].out, L.ray, r);
+    }
+};
+
+constexpr unsigned kFullMask = 0xffffffffu;
+
+__global__ void __launch_bounds__(256) cbq_k_flat_batch(const JobDesc* __restrict__ jobs, uint32_t njobs,
+                                                        uint64_t total, QueryParams q,
+                                                        unsigned long long* __restrict__ counter, uint32_t refill_min,
+                                                        uint32_t stack_rows)
+{
+    extern __shared__ uint32_t smem[];
+    SharedStack stack;
+    stack.base = smem + threadIdx.x;
+    stack.stride = blockDim.x;
+    uint64_t* prefix = reinterpret_cast<uint64_t*>(smem + (size_t)stack_rows * blockDim.x);
+    for (uint32_t j = threadIdx.x; j <= njobs; j += blockDim.x) prefix[j] = j < njobs ? jobs[j].first : total;
+    __syncthreads();
+
+    BatchSrc c;
+    c.jobs = jobs;
+    c.q = q;
+    const unsigned lane = threadIdx.x & 31u;
+    const uint32_t below = (1u << lane) - 1u;
+    Lane L;
+    L.mode = kLaneIdle;
+    L.job = 0;
+    L.nodes = nullptr;
+    bool more = true;
+    for (;;) {
+        if (more) {
+            const uint32_t idle = __ballot_sync(kFullMask, L.mode == kLaneIdle);
+            const uint32_t cnt = __popc(idle);
+            if (cnt == 32u || (cnt != 0u && cnt >= refill_min)) {
+                const int leader = __ffs(idle) - 1;
+                unsigned long long base = 0;
+                if ((int)lane == leader) base = atomicAdd(counter, (unsigned long long)cnt);
+                base = __shfl_sync(kFullMask, base, leader);
+                if (L.mode == kLaneIdle) {
+                    const uint64_t g = base + __popc(idle & below);
+                    if (g < total) {
+                        // Last job whose first ray is <= g (empty jobs are skipped).
+                        uint32_t lo = 0, hi = njobs;  // invariant: prefix[lo] <= g < prefix[hi]
+                        while (hi - lo > 1u) {
+                            const uint32_t mid = (lo + hi) >> 1;
+                            if (prefix[mid] <= g) lo = mid; else hi = mid;
+                        }
+                        L.job = lo;
+                        L.nodes = jobs[lo].nodes;
+                        lane_begin(L, c, g - prefix[lo]);
+                    }
+                }
+                if (base + cnt >= total) more = false;
+            }
+        }
+        if (!__any_sync(kFullMask, L.mode != kLaneIdle)) {
+            if (!more) break;
+            continue;
+        }
+        lane_settle(L, c);
+        if (L.mode == kLaneWalk) lane_walk(L, c, stack);
+    }
+}
+
+}  // namespace dev
+}  // namespace cbq
+
+using namespace cbq;
+
+namespace {
+constexpr int kBatchBlockDefault = 128;
+constexpr uint32_t kBatchRefillDefault = 8;
+}  // namespace
+
+struct cbq_batch {
+    int device = 0;
+    std::vector<cbq_job> jobs;              // as given (host copy)
+    std::vector<int> nested_jobs;           // jobs whose DAG needs the nested kernel
+    dev::JobDesc* d_jobs = nullptr;
+    uint32_t njobs = 0;                     // jobs in the device table
+    uint64_t total = 0;
+    uint32_t stack_rows = 1;
+    uint64_t* d_counter = nullptr;
+    cbq_query query{1, CBQ_MAX_FOOTPRINT_DISABLED, 0u, 0u};
+    int block = kBatchBlockDefault;
+    uint32_t refill = kBatchRefillDefault;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+cbq_status enqueue_batch(cbq_batch* b, cudaStream_t s)
+{
+    for (int j : b->nested_jobs) {
+        const cbq_job& jb = b->jobs[j];
+        cbq_status st = cbq_intersect(jb.dag, &jb.rays, jb.ray_count, &b->query, &jb.hits, (cbq_stream_t)s);
+        if (st != CBQ_OK) return st;
+    }
+    if (b->total == 0) return CBQ_OK;
+    if (cudaMemsetAsync(b->d_counter, 0, sizeof(uint64_t), s) != cudaSuccess) return CBQ_ERR_CUDA;
+    const size_t smem = (size_t)b->stack_rows * b->block * 4 + (size_t)(b->njobs + 1) * 8;
+    if (smem > 227u * 1024u) return CBQ_ERR_CAPACITY;
+    if (smem > 48u * 1024u &&
+        cudaFuncSetAttribute(dev::cbq_k_flat_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+        return CBQ_ERR_CUDA;
+    int sms = 0, per_sm = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device) != cudaSuccess) return CBQ_ERR_CUDA;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::cbq_k_flat_batch, b->block, smem) != cudaSuccess)
+        return CBQ_ERR_CUDA;
+    per_sm = std::max(per_sm, 1);
+    dev::QueryParams q;
+    q.compute_surface = b->query.compute_surface;
+    q.max_footprint = b->query.max_footprint;
+    q.flags = b->query.flags;
+    dev::cbq_k_flat_batch<<<sms * per_sm, b->block, smem, s>>>(b->d_jobs, b->njobs, b->total, q,
+                                                               (unsigned long long*)b->d_counter, b->refill,
+                                                               b->stack_rows);
+    return cudaGetLastError() == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
+}
+
+void drop_graph(cbq_batch* b)
+{
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+}
+
+cbq_status capture_graph(cbq_batch* b)
+{
+    drop_graph(b);
+    cudaStream_t s;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return CBQ_ERR_CUDA;
+    cudaGraph_t g = nullptr;
+    cbq_status st = CBQ_OK;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) st = CBQ_ERR_CUDA;
+    if (st == CBQ_OK) {
+        st = enqueue_batch(b, s);
+        if (cudaStreamEndCapture(s, &g) != cudaSuccess) st = CBQ_ERR_CUDA;
+    }
+    if (st == CBQ_OK && cudaGraphInstantiate(&b->exec, g, 0) != cudaSuccess) st = CBQ_ERR_CUDA;
+    if (g) cudaGraphDestroy(g);
+    cudaStreamDestroy(s);
+    if (st != CBQ_OK) {
+        cudaGetLastError();
+        b->exec = nullptr;
+    }
+    return st;
+}
+
+}  // namespace
+
+extern "C" {
+
+cbq_status cbq_batch_create(const cbq_job* jobs, int32_t job_count, const cbq_query* query, cbq_batch** out)
+{
+    if (!out || job_count < 0 || (job_count > 0 && !jobs)) return CBQ_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess) return CBQ_ERR_CUDA;
+    std::vector<dev::JobDesc> table;
+    cbq_batch* b = new (std::nothrow) cbq_batch();
+    if (!b) return CBQ_ERR_OUT_OF_MEMORY;
+    b->device = device;
+    if (query) b->query = *query;
+    uint64_t first = 0;
+    int32_t rows = 1;
+    for (int32_t j = 0; j < job_count; j++) {
+        const cbq_job& jb = jobs[j];
+        if (!jb.dag || jb.dag->device != device) { delete b; return CBQ_ERR_INVALID_ARGUMENT; }
+        if (jb.ray_count > 0 &&
+            (!jb.rays.origin_tmax || !jb.rays.direction || ((uintptr_t)jb.rays.origin_tmax & 15u) ||
+             ((uintptr_t)jb.rays.direction & 15u))) {
+            delete b;
+            return CBQ_ERR_INVALID_ARGUMENT;
+        }
+        b->jobs.push_back(jb);
+        if (jb.ray_count == 0) continue;
+        if (!jb.dag->flat_ok) { b->nested_jobs.push_back(j); continue; }
+        dev::JobDesc d;
+        std::memset(&d, 0, sizeof(d));
+        d.nodes = jb.dag->d_nodes;
+        d.orig = (const float4*)jb.rays.origin_tmax;
+        d.dir = (const float4*)jb.rays.direction;
+        d.out.hit = jb.hits.hit;
+        d.out.distance = jb.hits.distance;
+        d.out.material = jb.hits.material;
+        d.out.position = jb.hits.position;
+        d.out.normal = jb.hits.normal;
+        d.out.voxel = jb.hits.voxel;
+        d.out.status = jb.hits.status;
+        d.first = first;
+        d.count = jb.ray_count;
+        for (int k = 0; k < 8; k++) {
+            const cbq_subdag& s = jb.dag->subdags[k];
+            d.sd[k].lx = s.lower_bound[0];
+            d.sd[k].ly = s.lower_bound[1];
+            d.sd[k].lz = s.lower_bound[2];
+            d.sd[k].height = s.node_height;
+            d.sd[k].node = s.node_index;
+        }
+        table.push_back(d);
+        first += jb.ray_count;
+        rows = std::max(rows, jb.dag->max_height);
+    }
+    b->njobs = (uint32_t)table.size();
+    b->total = first;
+    b->stack_rows = (uint32_t)rows;
+    if (cudaMalloc((void**)&b->d_counter, 256 + table.size() * sizeof(dev::JobDesc)) != cudaSuccess) {
+        cudaGetLastError();
+        delete b;
+        return CBQ_ERR_OUT_OF_MEMORY;
+    }
+    b->d_jobs = (dev::JobDesc*)((char*)b->d_counter + 256);
+    if (!table.empty() &&
+        cudaMemcpy(b->d_jobs, table.data(), table.size() * sizeof(dev::JobDesc), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(b->d_counter);
+        delete b;
+        return CBQ_ERR_CUDA;
+    }
+    *out = b;
+    return CBQ_OK;
+}
+
+cbq_status cbq_batch_set_config(cbq_batch* b, int32_t block, uint32_t refill_min)
+{
+    if (!b || block < 0 || block > 256 || (block % 32) != 0 || refill_min > 32) return CBQ_ERR_INVALID_ARGUMENT;
+    b->block = block ? block : kBatchBlockDefault;
+    b->refill = refill_min ? refill_min : kBatchRefillDefault;
+    drop_graph(b);
+    return CBQ_OK;
+}
+
+cbq_status cbq_batch_get_config(const cbq_batch* b, int32_t* block, uint32_t* refill_min, uint64_t* total_rays)
+{
+    if (!b) return CBQ_ERR_INVALID_ARGUMENT;
+    if (block) *block = b->block;
+    if (refill_min) *refill_min = b->refill;
+    if (total_rays) *total_rays = b->total;
+    return CBQ_OK;
+}
+
+cbq_status cbq_batch_launch(cbq_batch* b, cbq_stream_t stream)
+{
+    if (!b) return CBQ_ERR_INVALID_ARGUMENT;
+    if (!b->exec) {
+        cbq_status st = capture_graph(b);
+        if (st != CBQ_OK) return st;
+    }
+    return cudaGraphLaunch(b->exec, (cudaStream_t)stream) == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
+}
+
+cbq_status cbq_batch_launch_direct(cbq_batch* b, cbq_stream_t stream)
+{
+    if (!b) return CBQ_ERR_INVALID_ARGUMENT;
+    return enqueue_batch(b, (cudaStream_t)stream);
+}
+
+cbq_status cbq_batch_autotune(cbq_batch* b, cbq_stream_t stream, int32_t repetitions)
+{
+    if (!b || repetitions <= 0) return CBQ_ERR_INVALID_ARGUMENT;
+    static const int blocks[] = {64, 128, 256};
+    static const uint32_t refills[] = {4, 8, 12, 16};
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return CBQ_ERR_CUDA;
+    float best = 1e30f;
+    int best_block = b->block;
+    uint32_t best_refill = b->refill;
+    cbq_status st = CBQ_OK;
+    for (int blk : blocks) {
+        for (uint32_t rf : refills) {
+            b->block = blk;
+            b->refill = rf;
+            st = enqueue_batch(b, (cudaStream_t)stream);  // warm-up
+            if (st != CBQ_OK) break;
+            cudaEventRecord(e0, (cudaStream_t)stream);
+            for (int r = 0; r < repetitions && st == CBQ_OK; r++) st = enqueue_batch(b, (cudaStream_t)stream);
+            cudaEventRecord(e1, (cudaStream_t)stream);
+            if (st != CBQ_OK || cudaEventSynchronize(e1) != cudaSuccess) { st = CBQ_ERR_CUDA; break; }
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best) { best = ms; best_block = blk; best_refill = rf; }
+        }
+        if (st != CBQ_OK) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->block = best_block;
+    b->refill = best_refill;
+    drop_graph(b);
+    return st;
+}
+
+cbq_status cbq_batch_destroy(cbq_batch* b)
+{
+    if (!b) return CBQ_ERR_INVALID_ARGUMENT;
+    drop_graph(b);
+    if (b->d_counter) cudaFree(b->d_counter);
+    delete b;
+    return CBQ_OK;
+}
+
+cbq_status cbq_intersect_batch(const cbq_job* jobs, int32_t job_count, const cbq_query* query, cbq_stream_t stream)
+{
+    cbq_batch* b = nullptr;
+    cbq_status st = cbq_batch_create(jobs, job_count, query, &b);
+    if (st != CBQ_OK) return st;
+    st = enqueue_batch(b, (cudaStream_t)stream);
+    if (st == CBQ_OK && cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess) st = CBQ_ERR_CUDA;
+    cbq_batch_destroy(b);
+    return st;
+}
+
+}  // extern "C"

@@ -37,9 +37,14 @@ struct Lane {
     int h, start_h;
     float last_exit;
     uint32_t fetches, status, mode;
-    uint64_t ray;
+    uint32_t job;                // batch kernel: index of the lane's job
+    uint64_t ray;                // ray index within its job
+    const uint32_t* nodes;       // batch kernel: the job's node store
 };
 
+// Where a lane's volume, rays and outputs are.  The lane functions below are
+// templates over this "source" so that the single-volume kernel and the
+// multi-volume batch kernel share the same arithmetic.
 struct FlatCtx {
     DagParams dag;
     QueryParams q;
@@ -47,6 +52,16 @@ struct FlatCtx {
     const float4* __restrict__ orig;
     const float4* __restrict__ dir;
     uint32_t* __restrict__ fetch_out;
+
+    __device__ __forceinline__ const uint32_t* nodes(const Lane&) const { return dag.nodes; }
+    __device__ __forceinline__ const SubDag& subdag(const Lane&, uint32_t k) const { return dag.sd[k]; }
+    __device__ __forceinline__ float4 ray_origin(const Lane&, uint64_t i) const { return __ldg(orig + i); }
+    __device__ __forceinline__ float4 ray_direction(const Lane&, uint64_t i) const { return __ldg(dir + i); }
+    __device__ __forceinline__ void write(const Lane& L, const RayResult& r) const
+    {
+        write_result(out, L.ray, r);
+        if (fetch_out) fetch_out[L.ray] = L.fetches;
+    }
 };
 
 __device__ __forceinline__ uint32_t first_child_f(const Lane& L, float entry, float fcx, float fcy, float fcz)
@@ -62,11 +77,12 @@ __device__ __forceinline__ uint32_t first_child_f(const Lane& L, float entry, fl
 }
 
 // Per-ray set-up: intersectVolume up to the octant loop (raytracing.cpp:409-434).
-__device__ __forceinline__ void lane_begin(Lane& L, const FlatCtx& c, uint64_t i)
+template <typename Src>
+__device__ __forceinline__ void lane_begin(Lane& L, const Src& c, uint64_t i)
 {
     L.ray = i;
-    L.o = __ldg(c.orig + i);
-    L.d = __ldg(c.dir + i);
+    L.o = c.ray_origin(L, i);
+    L.d = c.ray_direction(L, i);
     const uint32_t sbx = L.d.x < 0.0f, sby = L.d.y < 0.0f, sbz = L.d.z < 0.0f;
     L.sign = sbx | (sby << 1) | (sbz << 2);
     const float sx = sbx ? -1.0f : 1.0f, sy = sby ? -1.0f : 1.0f, sz = sbz ? -1.0f : 1.0f;
@@ -90,7 +106,8 @@ __device__ __forceinline__ void lane_begin(Lane& L, const FlatCtx& c, uint64_t i
 }
 
 // Writes the result of ray L.ray and frees the lane.
-__device__ __forceinline__ void lane_finish(Lane& L, const FlatCtx& c, bool hit, float dist, uint32_t material,
+template <typename Src>
+__device__ __forceinline__ void lane_finish(Lane& L, const Src& c, bool hit, float dist, uint32_t material,
                                             float nx, float ny, float nz)
 {
     RayResult r;
@@ -114,13 +131,13 @@ __device__ __forceinline__ void lane_finish(Lane& L, const FlatCtx& c, bool hit,
         r.px = r.py = r.pz = 0.0f;
         r.nx = r.ny = r.nz = 0.0f;
     }
-    write_result(c.out, L.ray, r);
-    if (c.fetch_out) c.fetch_out[L.ray] = L.fetches;
+    c.write(L, r);
     L.mode = kLaneIdle;
 }
 
 // One octant transition (raytracing.cpp:469-475).
-__device__ __forceinline__ void lane_next(Lane& L, const FlatCtx& c)
+template <typename Src>
+__device__ __forceinline__ void lane_next(Lane& L, const Src& c)
 {
     const float md = min3_ref(L.ddx, L.ddy, L.ddz);
     const uint32_t before = L.oct;
@@ -139,9 +156,10 @@ __device__ __forceinline__ void lane_next(Lane& L, const FlatCtx& c)
 
 // Enters the SubDAG of the current octant: the slab test and set-up at the top
 // of intersectRayNodeESVO (raytracing.cpp:218-250, 443-460).
-__device__ __forceinline__ void lane_enter(Lane& L, const FlatCtx& c)
+template <typename Src>
+__device__ __forceinline__ void lane_enter(Lane& L, const Src& c)
 {
-    const SubDag& s = c.dag.sd[L.oct ^ L.sign];
+    const SubDag& s = c.subdag(L, L.oct ^ L.sign);
     if (s.node == 0u) {
         L.mode = kLaneNext;
         return;
@@ -182,8 +200,8 @@ __device__ __forceinline__ void lane_enter(Lane& L, const FlatCtx& c)
 }
 
 // One iteration of the ESVO loop (raytracing.cpp:253-367).
-template <typename Stack>
-__device__ __forceinline__ void lane_walk(Lane& L, const FlatCtx& c, Stack& stack)
+template <typename Src, typename Stack>
+__device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
 {
     const float c1x = ((L.fx + L.fcns) - L.rox) * L.ix;
     const float c1y = ((L.fy + L.fcns) - L.roy) * L.iy;
@@ -194,7 +212,7 @@ __device__ __forceinline__ void lane_walk(Lane& L, const FlatCtx& c, Stack& stac
         lane_finish(L, c, false, 0.0f, 0u, 0.0f, 0.0f, 0.0f);
         return;
     }
-    const uint32_t child = load_child(c.dag.nodes, L.node, L.cid ^ L.sign);
+    const uint32_t child = load_child(c.nodes(L), L.node, L.cid ^ L.sign);
     L.fetches++;
     if (child > 0u) {
         const float c0x = (L.fx - L.rox) * L.ix;
@@ -219,7 +237,7 @@ __device__ __forceinline__ void lane_walk(Lane& L, const FlatCtx& c, Stack& stac
             uint32_t material = 0u;
             float nx = 0.0f, ny = 0.0f, nz = 0.0f;
             if (c.q.compute_surface) {
-                material = nearest_material(c.dag.nodes, child, L.sign, L.fetches, L.status);
+                material = nearest_material(c.nodes(L), child, L.sign, L.fetches, L.status);
                 if (L.status != kRayOk) {
                     lane_finish(L, c, false, 0.0f, 0u, 0.0f, 0.0f, 0.0f);
                     return;
@@ -270,7 +288,8 @@ __device__ __forceinline__ void lane_walk(Lane& L, const FlatCtx& c, Stack& stac
 // Octant transitions until the lane walks a SubDAG or has finished.  Bounded:
 // every kLaneNext raises `oct` (or finishes the ray), every kLaneEnter walks or
 // moves on, so at most 16 transitions happen.
-__device__ __forceinline__ void lane_settle(Lane& L, const FlatCtx& c)
+template <typename Src>
+__device__ __forceinline__ void lane_settle(Lane& L, const Src& c)
 {
     while (L.mode == kLaneEnter || L.mode == kLaneNext) {
         if (L.mode == kLaneNext)

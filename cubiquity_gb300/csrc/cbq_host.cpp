@@ -315,6 +315,35 @@ static inline uint64_t splitmix(uint64_t x)
     return x ^ (x >> 31);
 }
 
+cbq_status cbq_gen_sphere_rays(const double lo[3], const double hi[3], uint64_t n, uint64_t seed, float* origin_tmax,
+                                float* direction)
+{
+    if (!lo || !hi || !origin_tmax || !direction) return CBQ_ERR_INVALID_ARGUMENT;
+    for (uint64_t i = 0; i < n; i++) {
+        uint64_t ctr = splitmix(seed ^ splitmix(i * 0x9e3779b97f4a7c15ull + 17));
+        for (int a = 0; a < 3; a++) {
+            ctr = splitmix(ctr);
+            const double u = (double)(ctr >> 11) * (1.0 / 9007199254740992.0);
+            origin_tmax[4 * i + a] = (float)(lo[a] + (hi[a] - lo[a]) * u);
+        }
+        origin_tmax[4 * i + 3] = std::numeric_limits<float>::infinity();
+        for (;;) {
+            double q[3];
+            for (int a = 0; a < 3; a++) {
+                ctr = splitmix(ctr);
+                q[a] = (double)(ctr >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+            }
+            const double q2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
+            if (q2 >= 1.0 || q2 < 1e-6) continue;
+            const double ql = std::sqrt(q2);
+            for (int a = 0; a < 3; a++) direction[4 * i + a] = (float)(q[a] / ql);
+            break;
+        }
+        direction[4 * i + 3] = 0.0f;
+    }
+    return CBQ_OK;
+}
+
 cbq_status cbq_gen_bounce_rays(const float* hit_position, const float* hit_normal, uint64_t hit_count, uint64_t n,
                                uint64_t seed, float* origin_tmax, float* direction)
 {

@@ -73,6 +73,56 @@ def camera_scaled(edge_log2: int, width: int, height: int) -> CameraSpec:
                       width, height)
 
 
+@dataclass(frozen=True)
+class BatchVolume:
+    """One volume of the batching workload and its ray batch: `pinhole` camera
+    rays at the volume plus `interior` rays from uniform interior points in
+    uniform directions."""
+    scene: SceneSpec
+    camera: CameraSpec
+    interior: int
+    ray_seed: int
+
+    @property
+    def rays(self) -> int:
+        return self.camera.width * self.camera.height + self.interior
+
+    def make_rays(self):
+        o1, d1 = self.camera.rays()
+        e = float(1 << self.scene.edge_log2)
+        o2, d2 = cbq.sphere_rays((0.0, 0.0, 0.0), (e, e, e), self.interior, self.ray_seed)
+        return np.concatenate([o1, o2]), np.concatenate([d1, d2])
+
+
+def batch_volumes(count: int = 64, seed: int = 20240610, edge_log2=(7, 11), rays=(16384, 1 << 20)):
+    """The batching workload: `count` volumes of edge 2^k, k uniform in
+    edge_log2, each a seeded sphere or terrain scene, each with a ray batch of
+    log-uniform size in `rays`, half pinhole rays at the volume and half rays
+    from uniform interior points in uniform directions.  Deterministic on every
+    machine (Python's Mersenne Twister; scenes and rays come from libcbq)."""
+    import math
+    import random
+
+    rng = random.Random(seed)
+    out = []
+    for i in range(count):
+        k = rng.randint(edge_log2[0], edge_log2[1])
+        kind = cbq.SCENE_SPHERES if rng.random() < 0.5 else cbq.SCENE_TERRAIN
+        scene = SceneSpec(kind, k, seed * 1000 + i, 64 if kind == cbq.SCENE_SPHERES else 0)
+        n = int(round(math.exp(rng.uniform(math.log(rays[0]), math.log(rays[1])))))
+        w = max(1, int(math.isqrt(n // 2)))
+        h = max(1, (n // 2) // w)
+        e = float(1 << k)
+        theta = rng.uniform(0.0, 2.0 * math.pi)
+        phi = rng.uniform(0.15, 1.2)  # elevation above the horizon
+        c = (e / 2, e / 2, e / 4)
+        r = 1.6 * e
+        eye = (c[0] + r * math.cos(phi) * math.cos(theta), c[1] + r * math.cos(phi) * math.sin(theta),
+               c[2] + r * math.sin(phi))
+        out.append(BatchVolume(scene, CameraSpec(eye, c, w, h), n - w * h, seed * 7919 + i))
+    return out
+
+
 def bounce_from_hits(hits: dict, n: int, seed: int = TERRAIN_BOUNCE_SEED):
     """Bounce rays from the hits of a primary pass (host arrays or tensors)."""
     hit = _np(hits["hit"]).astype(bool)

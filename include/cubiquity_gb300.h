@@ -199,6 +199,40 @@ cbq_status cbq_intersect_persistent(const cbq_dag* dag, const cbq_rays* rays, ui
                                     const cbq_query* query, const cbq_hits* hits,
                                     uint64_t* work_counter, uint32_t chunk, cbq_stream_t stream);
 
+/* ------------------------------------------------------- batched form */
+
+/* One volume and its ray batch (device buffers). */
+typedef struct cbq_job {
+    const cbq_dag* dag;
+    cbq_rays rays;
+    uint64_t ray_count;
+    cbq_hits hits;
+} cbq_job;
+
+/* A prepared batch: many volumes of uneven size and ray batches of uneven
+ * length traversed by ONE persistent launch (a job table in device memory;
+ * warps refill idle lanes from a single work counter), captured in a CUDA
+ * graph on first launch and replayed after.  Results equal cbq_intersect on
+ * each job alone.  The job arrays must stay valid while the batch exists. */
+typedef struct cbq_batch cbq_batch;
+
+cbq_status cbq_batch_create(const cbq_job* jobs, int32_t job_count, const cbq_query* query, cbq_batch** out);
+/* block: threads per block (32..256, 0 = default); refill_min: idle lanes that
+ * trigger a warp's refill (1..32, 0 = default).  Re-captures on next launch. */
+cbq_status cbq_batch_set_config(cbq_batch* b, int32_t block, uint32_t refill_min);
+cbq_status cbq_batch_get_config(const cbq_batch* b, int32_t* block, uint32_t* refill_min, uint64_t* total_rays);
+/* Times the candidate launch shapes on this batch (synchronous) and keeps the
+ * fastest. */
+cbq_status cbq_batch_autotune(cbq_batch* b, cbq_stream_t stream, int32_t repetitions);
+/* Replays the captured graph on `stream` (captures it first if needed). */
+cbq_status cbq_batch_launch(cbq_batch* b, cbq_stream_t stream);
+/* The same work launched directly, without the graph. */
+cbq_status cbq_batch_launch_direct(cbq_batch* b, cbq_stream_t stream);
+cbq_status cbq_batch_destroy(cbq_batch* b);
+/* One-shot: create, launch on `stream`, wait, destroy. */
+cbq_status cbq_intersect_batch(const cbq_job* jobs, int32_t job_count, const cbq_query* query,
+                               cbq_stream_t stream);
+
 /* Statistics form of cbq_intersect: writes only the number of node fetches
  * (dependent child loads) each ray performed to the device array `fetches`. */
 cbq_status cbq_count_fetches(const cbq_dag* dag, const cbq_rays* rays, uint64_t n,
@@ -255,6 +289,11 @@ cbq_status cbq_dag_reorder_bfs(const uint32_t* nodes, uint64_t node_count, uint3
  * tan_half_fov = tan(vertical fov / 2); z is up. */
 cbq_status cbq_gen_pinhole_rays(const double eye[3], const double target[3], double tan_half_fov,
                                 int32_t width, int32_t height, float* origin_tmax, float* direction);
+
+/* Rays with origins uniform in the box [lo, hi] and directions uniform on the
+ * unit sphere, from a counter-based hash of (seed, i); same floats everywhere. */
+cbq_status cbq_gen_sphere_rays(const double lo[3], const double hi[3], uint64_t n, uint64_t seed,
+                               float* origin_tmax, float* direction);
 
 /* Cosine-weighted bounce rays: ray i starts at hit (i mod hit_count) at
  * position + 0.01 * normal (pathtracing_demo.cpp:166) with direction
