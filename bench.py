@@ -50,7 +50,8 @@ def parse_args():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    p.add_argument("--workload", choices=["terrain-4096", "spheres-256", "batch-64"], default="terrain-4096")
+    p.add_argument("--workload", choices=["terrain-4096", "spheres-256", "batch-64", "serve-8"],
+                   default="terrain-4096")
     p.add_argument("--kernel", choices=["auto", "flat", "nested"], default="auto")
     p.add_argument("--form", choices=["persistent", "plain"], default="persistent",
                    help="persistent grid pulling rays from a work counter, or one thread per ray")
@@ -586,6 +587,130 @@ def run_gpu_batch(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def run_gpu_serve(args, world, rank, local):
+    """configs[3]: 8 resident terrain DAGs (edges 1024-4096); requests of 1k-256k
+    rays (log-uniform), 70% tmax-bounded collision rays and 30% view rays.
+    Finds the peak request rate closed-loop, then drives an open-loop Poisson
+    stream at half of it and reports p50/p99 latency (submit -> hits in host
+    memory, timed by the server) and Mrays/s."""
+    import random
+    import threading
+    import torch
+    import cubiquity_gb300 as cbq
+    from cubiquity_gb300 import workloads as W
+
+    torch.cuda.set_device(local)
+    scenes = W.serve_volumes()
+    dags, pools = [], []
+    for i, s in enumerate(scenes):
+        nodes, root = s.build()
+        dags.append(cbq.Dag(nodes, root))
+        (co, cd), (vo, vd) = W.serve_ray_pools(s, 1 << 19, 724, 7000 + i)
+        pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
+        pools.append(((pin(co), pin(cd)), (pin(vo), pin(vd))))
+    sizes = (1 << 19, 724 * 724)
+    reqs = W.serve_requests(20000, sizes, seed=1234)
+    ring = 64
+    max_n = 262144
+    outs = [{"hit": torch.empty(max_n, dtype=torch.uint8).pin_memory().numpy(),
+             "distance": torch.empty(max_n, dtype=torch.float32).pin_memory().numpy(),
+             "material": torch.empty(max_n, dtype=torch.int32).pin_memory().numpy(),
+             "voxel": torch.empty((max_n, 3), dtype=torch.int32).pin_memory().numpy(),
+             "status": torch.empty(max_n, dtype=torch.uint8).pin_memory().numpy()} for _ in range(ring)]
+    server = cbq.Server(device_memory_budget=2 << 30, max_inflight_launches=4, max_batch_requests=128,
+                        max_batch_rays=4 << 20)
+    queries = {True: cbq.Query(True, cbq.MAX_FOOTPRINT_DISABLED, True), False: cbq.Query()}
+
+    def submit(k, r):
+        (co, cd), (vo, vd) = pools[r.volume]
+        o, d = (co, cd) if r.collision else (vo, vd)
+        out = {f: v[: r.count] for f, v in outs[k % ring].items()}
+        t, _ = server.submit(dags[r.volume], o[r.start:r.start + r.count], d[r.start:r.start + r.count],
+                             queries[r.collision], out=out)
+        return t
+
+    # Peak: closed loop with up to `ring` requests outstanding for a fixed count.
+    def closed_loop(first, count):
+        pending = []
+        t0 = time.perf_counter()
+        for k in range(first, first + count):
+            if len(pending) >= ring:
+                server.wait(pending.pop(0))
+            pending.append(submit(k, reqs[k % len(reqs)]))
+        for t in pending:
+            server.wait(t)
+        return time.perf_counter() - t0
+
+    closed_loop(0, 300)  # warm-up
+    server.reset_stats()
+    n_peak = 3000
+    dt = closed_loop(300, n_peak)
+    peak = server.stats()
+    peak_rps = n_peak / dt
+    peak_mrays = peak["rays_completed"] / dt / 1e6
+
+    def open_loop(rate, duration, first):
+        """Poisson arrivals at `rate` requests/s for `duration` seconds."""
+        rng = random.Random(rate)
+        times, t = [], 0.0
+        while t < duration:
+            t += rng.expovariate(rate)
+            times.append(t)
+        tickets = [None] * len(times)
+        done = threading.Semaphore(ring)
+        issued = threading.Event()
+
+        def waiter():
+            for i in range(len(times)):
+                while tickets[i] is None:
+                    time.sleep(0)
+                server.wait(tickets[i])
+                done.release()
+
+        server.reset_stats()
+        th = threading.Thread(target=waiter)
+        th.start()
+        backpressure = 0
+        t0 = time.perf_counter()
+        for i, at in enumerate(times):
+            while time.perf_counter() - t0 < at:
+                pass
+            if not done.acquire(blocking=False):
+                backpressure += 1
+                done.acquire()
+            tickets[i] = submit(first + i, reqs[(first + i) % len(reqs)])
+        th.join()
+        wall = time.perf_counter() - t0
+        st = server.stats()
+        return {"rate_rps": rate, "requests": len(times), "p50_ms": st["latency_p50_us"] / 1e3,
+                "p99_ms": st["latency_p99_us"] / 1e3, "max_ms": st["latency_max_us"] / 1e3,
+                "mrays_per_s": st["rays_completed"] / wall / 1e6, "requests_per_launch": st["mean_requests_per_launch"],
+                "generator_backpressure": backpressure}
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    half = open_loop(0.5 * peak_rps, 4.0, 5000)
+    clk = clocks.stop()
+    sweep = [open_loop(f * peak_rps, 2.0, 9000 + int(f * 1000)) for f in (0.25, 0.75)]
+    server.close()
+    line = {
+        "metric": "p99 latency at 50% of peak load", "value": half["p99_ms"], "unit": "ms", "n_gpus": world,
+        "steps": half["requests"], "warmup": 300, "ms_per_step": half["p50_ms"], "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (8 seeded terrain DAGs, 1k-256k-ray requests: 70% collision tmax<=64, 30% view)",
+        "config": {"workload": "serve-8", "edges": [1 << s.edge_log2 for s in scenes],
+                   "server": {"memory_budget_gb": 2, "inflight_launches": 4, "max_batch_requests": 128},
+                   "arrivals": "open-loop Poisson"},
+        "peak": {"requests_per_s": peak_rps, "mrays_per_s": peak_mrays, "p50_ms": peak["latency_p50_us"] / 1e3,
+                 "p99_ms": peak["latency_p99_us"] / 1e3},
+        "half_load": half, "sweep": sweep,
+        "e2e": {"value": half["mrays_per_s"], "unit": "Mrays/s", "note": "host rays in, host hits out, per request"},
+        "gpu_launches": None, "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     world, rank, local = dist_setup(args)
@@ -596,6 +721,8 @@ def main():
             run_reference(args, world, rank)
     elif args.workload == "batch-64":
         run_gpu_batch(args, world, rank, local)
+    elif args.workload == "serve-8":
+        run_gpu_serve(args, world, rank, local)
     else:
         run_gpu(args, world, rank, local)
     if world > 1:

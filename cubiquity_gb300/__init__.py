@@ -469,6 +469,100 @@ def intersect_volume_host(dag: Dag, origin_tmax: np.ndarray, direction: np.ndarr
     return out
 
 
+# ------------------------------------------------------------ serving
+
+class _Request(ctypes.Structure):
+    _fields_ = [("dag", ctypes.c_void_p), ("host_origin_tmax", ctypes.c_void_p), ("host_direction", ctypes.c_void_p),
+                ("ray_count", ctypes.c_uint64), ("query", _Query), ("host_hits", _Hits)]
+
+
+class _ServerConfig(ctypes.Structure):
+    _fields_ = [("device_memory_budget", ctypes.c_uint64), ("max_inflight_launches", ctypes.c_int32),
+                ("max_batch_requests", ctypes.c_int32), ("max_batch_rays", ctypes.c_uint64),
+                ("block", ctypes.c_int32), ("refill_min", ctypes.c_uint32)]
+
+
+class _ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("rays_completed", ctypes.c_uint64),
+                ("launches", ctypes.c_uint64), ("queued", ctypes.c_uint64), ("inflight_launches", ctypes.c_uint64),
+                ("mean_requests_per_launch", ctypes.c_double), ("latency_p50_us", ctypes.c_double),
+                ("latency_p99_us", ctypes.c_double), ("latency_max_us", ctypes.c_double),
+                ("latency_mean_us", ctypes.c_double), ("busy_seconds", ctypes.c_double)]
+
+
+_sig("cbq_server_create", [ctypes.POINTER(_ServerConfig), ctypes.POINTER(_P)])
+_sig("cbq_server_submit", [_P, ctypes.POINTER(_Request), ctypes.POINTER(_U64)])
+_sig("cbq_server_wait", [_P, _U64, ctypes.c_int64])
+_sig("cbq_server_poll", [_P, _U64, ctypes.POINTER(ctypes.c_int32)])
+_sig("cbq_server_get_stats", [_P, ctypes.POINTER(_ServerStats)])
+_sig("cbq_server_reset_stats", [_P])
+_sig("cbq_server_destroy", [_P])
+
+
+class Server:
+    """Continuous-batching request server over resident DAGs (cbq_server).
+
+    submit() takes host numpy arrays and returns a ticket at once; the arrays
+    are kept alive here until the ticket is waited for."""
+
+    def __init__(self, device_memory_budget: int = 1 << 30, max_inflight_launches: int = 4,
+                 max_batch_requests: int = 256, max_batch_rays: int = 4 << 20, block: int = 0, refill_min: int = 0):
+        cfg = _ServerConfig(device_memory_budget, max_inflight_launches, max_batch_requests, max_batch_rays, block,
+                            refill_min)
+        h = _P()
+        _check(_lib.cbq_server_create(ctypes.byref(cfg), ctypes.byref(h)), "cbq_server_create")
+        self._h = h
+        self._keep = {}
+
+    def submit(self, dag: Dag, origin_tmax: np.ndarray, direction: np.ndarray, query: Query | None = None,
+               out: dict | None = None):
+        """Queues one request; returns (ticket, out) where `out` receives the hits."""
+        o = np.ascontiguousarray(origin_tmax, dtype=np.float32).reshape(-1, 4)
+        d = np.ascontiguousarray(direction, dtype=np.float32).reshape(-1, 4)
+        n = o.shape[0]
+        if out is None:
+            out = alloc_host_hits(n)
+        req = _Request(dag.handle, _np_ptr(o), _np_ptr(d), n, (query or Query()).c(),
+                       _Hits(*[_np_ptr(out.get(k)) for k in HIT_FIELDS]))
+        t = _U64()
+        _check(_lib.cbq_server_submit(self._h, ctypes.byref(req), ctypes.byref(t)), "cbq_server_submit")
+        self._keep[t.value] = (o, d, out, dag)
+        return t.value, out
+
+    def wait(self, ticket: int, timeout_us: int = -1) -> int:
+        """Status of the request (0 = ok); raises CbqError on timeout or failure."""
+        st = _lib.cbq_server_wait(self._h, ticket, timeout_us)
+        if st != 5:  # not a timeout: the request is finished (or unknown)
+            self._keep.pop(ticket, None)
+        _check(st, "cbq_server_wait")
+        return st
+
+    def poll(self, ticket: int) -> bool:
+        done = ctypes.c_int32()
+        _check(_lib.cbq_server_poll(self._h, ticket, ctypes.byref(done)), "cbq_server_poll")
+        return bool(done.value)
+
+    def stats(self) -> dict:
+        s = _ServerStats()
+        _check(_lib.cbq_server_get_stats(self._h, ctypes.byref(s)), "cbq_server_get_stats")
+        return {name: getattr(s, name) for name, _ in _ServerStats._fields_}
+
+    def reset_stats(self) -> None:
+        _check(_lib.cbq_server_reset_stats(self._h), "cbq_server_reset_stats")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            _lib.cbq_server_destroy(self._h)
+            self._h = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 # ------------------------------------------------------------ batched form
 
 class Batch:

@@ -2,14 +2,12 @@
 // persistent launch, captured in a CUDA graph and replayed (cbq_batch_*).
 //
 // A job table in device memory holds, per job, the node store, the SubDAGs, the
-// ray and hit arrays and the job's first global ray index.  Persistent warps
-// take global ray indices from one atomic counter (warp-aggregated refill of
-// idle lanes, as in the single-volume persistent kernel); a lane finds its job
-// by binary search over the prefix offsets, held in shared memory.
-#include "cbq_flat.cuh"
-#include "cbq_internal.hpp"
-
-#include <cuda_runtime.h>
+// ray and hit arrays, the query and the job's first global ray index.
+// Persistent warps take global ray indices from one atomic counter
+// (warp-aggregated refill of idle lanes, as in the single-volume persistent
+// kernel); a lane finds its job by binary search over the prefix offsets, held
+// in shared memory.
+#include "cbq_batch.cuh"
 
 #include <algorithm>
 #include <cstring>
@@ -19,20 +17,10 @@
 namespace cbq {
 namespace dev {
 
-struct JobDesc {
-    const uint32_t* nodes;
-    const float4* orig;
-    const float4* dir;
-    HitsOut out;
-    uint64_t first;   // global index of the job's first ray
-    uint64_t count;
-    SubDag sd[8];
-};
-
 struct BatchSrc {
     const JobDesc* __restrict__ jobs;
-    QueryParams q;
 
+    __device__ __forceinline__ const QueryParams& query(const Lane& L) const { return jobs[L.job].q; }
     __device__ __forceinline__ const uint32_t* nodes(const Lane& L) const { return L.nodes; }
     __device__ __forceinline__ const SubDag& subdag(const Lane& L, uint32_t k) const { return jobs[L.job].sd[k]; }
     __device__ __forceinline__ float4 ray_origin(const Lane& L, uint64_t i) const { return __ldg(jobs[L.job].orig + i); }
@@ -46,9 +34,8 @@ struct BatchSrc {
 constexpr unsigned kFullMask = 0xffffffffu;
 
 __global__ void __launch_bounds__(256) cbq_k_flat_batch(const JobDesc* __restrict__ jobs, uint32_t njobs,
-                                                        uint64_t total, QueryParams q,
-                                                        unsigned long long* __restrict__ counter, uint32_t refill_min,
-                                                        uint32_t stack_rows)
+                                                        uint64_t total, unsigned long long* __restrict__ counter,
+                                                        uint32_t refill_min, uint32_t stack_rows)
 {
     extern __shared__ uint32_t smem[];
     SharedStack stack;
@@ -60,7 +47,6 @@ __global__ void __launch_bounds__(256) cbq_k_flat_batch(const JobDesc* __restric
 
     BatchSrc c;
     c.jobs = jobs;
-    c.q = q;
     const unsigned lane = threadIdx.x & 31u;
     const uint32_t below = (1u << lane) - 1u;
     Lane L;
@@ -80,8 +66,9 @@ __global__ void __launch_bounds__(256) cbq_k_flat_batch(const JobDesc* __restric
                 if (L.mode == kLaneIdle) {
                     const uint64_t g = base + __popc(idle & below);
                     if (g < total) {
-                        // Last job whose first ray is <= g (empty jobs are skipped).
-                        uint32_t lo = 0, hi = njobs;  // invariant: prefix[lo] <= g < prefix[hi]
+                        // Last job whose first ray is <= g.  Every job in the
+                        // table has at least one ray.
+                        uint32_t lo = 0, hi = njobs;  // prefix[lo] <= g < prefix[hi]
                         while (hi - lo > 1u) {
                             const uint32_t mid = (lo + hi) >> 1;
                             if (prefix[mid] <= g) lo = mid; else hi = mid;
@@ -104,6 +91,42 @@ __global__ void __launch_bounds__(256) cbq_k_flat_batch(const JobDesc* __restric
 }
 
 }  // namespace dev
+
+void fill_job_volume(dev::JobDesc& d, const cbq_dag* dag)
+{
+    d.nodes = dag->d_nodes;
+    for (int k = 0; k < 8; k++) {
+        const cbq_subdag& s = dag->subdags[k];
+        d.sd[k].lx = s.lower_bound[0];
+        d.sd[k].ly = s.lower_bound[1];
+        d.sd[k].lz = s.lower_bound[2];
+        d.sd[k].height = s.node_height;
+        d.sd[k].node = s.node_index;
+        d.sd[k].pad[0] = d.sd[k].pad[1] = d.sd[k].pad[2] = 0;
+    }
+}
+
+cbq_status launch_batch_kernel(const dev::JobDesc* d_jobs, uint32_t njobs, uint64_t total, uint64_t* counter,
+                               int block, uint32_t refill, uint32_t stack_rows, int device, cudaStream_t s)
+{
+    if (total == 0 || njobs == 0) return CBQ_OK;
+    if (cudaMemsetAsync(counter, 0, sizeof(uint64_t), s) != cudaSuccess) return CBQ_ERR_CUDA;
+    const size_t smem = (size_t)stack_rows * block * 4 + (size_t)(njobs + 1) * 8;
+    if (smem > 227u * 1024u) return CBQ_ERR_CAPACITY;
+    if (smem > 48u * 1024u &&
+        cudaFuncSetAttribute(dev::cbq_k_flat_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+        return CBQ_ERR_CUDA;
+    int sms = 0, per_sm = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return CBQ_ERR_CUDA;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::cbq_k_flat_batch, block, smem) != cudaSuccess)
+        return CBQ_ERR_CUDA;
+    per_sm = std::max(per_sm, 1);
+    dev::cbq_k_flat_batch<<<sms * per_sm, block, smem, s>>>(d_jobs, njobs, total, (unsigned long long*)counter,
+                                                            refill, stack_rows);
+    return cudaGetLastError() == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
+}
+
 }  // namespace cbq
 
 using namespace cbq;
@@ -137,27 +160,8 @@ cbq_status enqueue_batch(cbq_batch* b, cudaStream_t s)
         cbq_status st = cbq_intersect(jb.dag, &jb.rays, jb.ray_count, &b->query, &jb.hits, (cbq_stream_t)s);
         if (st != CBQ_OK) return st;
     }
-    if (b->total == 0) return CBQ_OK;
-    if (cudaMemsetAsync(b->d_counter, 0, sizeof(uint64_t), s) != cudaSuccess) return CBQ_ERR_CUDA;
-    const size_t smem = (size_t)b->stack_rows * b->block * 4 + (size_t)(b->njobs + 1) * 8;
-    if (smem > 227u * 1024u) return CBQ_ERR_CAPACITY;
-    if (smem > 48u * 1024u &&
-        cudaFuncSetAttribute(dev::cbq_k_flat_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-            cudaSuccess)
-        return CBQ_ERR_CUDA;
-    int sms = 0, per_sm = 0;
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device) != cudaSuccess) return CBQ_ERR_CUDA;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::cbq_k_flat_batch, b->block, smem) != cudaSuccess)
-        return CBQ_ERR_CUDA;
-    per_sm = std::max(per_sm, 1);
-    dev::QueryParams q;
-    q.compute_surface = b->query.compute_surface;
-    q.max_footprint = b->query.max_footprint;
-    q.flags = b->query.flags;
-    dev::cbq_k_flat_batch<<<sms * per_sm, b->block, smem, s>>>(b->d_jobs, b->njobs, b->total, q,
-                                                               (unsigned long long*)b->d_counter, b->refill,
-                                                               b->stack_rows);
-    return cudaGetLastError() == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
+    return launch_batch_kernel(b->d_jobs, b->njobs, b->total, b->d_counter, b->block, b->refill, b->stack_rows,
+                               b->device, s);
 }
 
 void drop_graph(cbq_batch* b)
@@ -219,7 +223,7 @@ cbq_status cbq_batch_create(const cbq_job* jobs, int32_t job_count, const cbq_qu
         if (!jb.dag->flat_ok) { b->nested_jobs.push_back(j); continue; }
         dev::JobDesc d;
         std::memset(&d, 0, sizeof(d));
-        d.nodes = jb.dag->d_nodes;
+        fill_job_volume(d, jb.dag);
         d.orig = (const float4*)jb.rays.origin_tmax;
         d.dir = (const float4*)jb.rays.direction;
         d.out.hit = jb.hits.hit;
@@ -231,14 +235,9 @@ cbq_status cbq_batch_create(const cbq_job* jobs, int32_t job_count, const cbq_qu
         d.out.status = jb.hits.status;
         d.first = first;
         d.count = jb.ray_count;
-        for (int k = 0; k < 8; k++) {
-            const cbq_subdag& s = jb.dag->subdags[k];
-            d.sd[k].lx = s.lower_bound[0];
-            d.sd[k].ly = s.lower_bound[1];
-            d.sd[k].lz = s.lower_bound[2];
-            d.sd[k].height = s.node_height;
-            d.sd[k].node = s.node_index;
-        }
+        d.q.compute_surface = b->query.compute_surface;
+        d.q.max_footprint = b->query.max_footprint;
+        d.q.flags = b->query.flags;
         table.push_back(d);
         first += jb.ray_count;
         rows = std::max(rows, jb.dag->max_height);

@@ -53,6 +53,7 @@ struct FlatCtx {
     const float4* __restrict__ dir;
     uint32_t* __restrict__ fetch_out;
 
+    __device__ __forceinline__ const QueryParams& query(const Lane&) const { return q; }
     __device__ __forceinline__ const uint32_t* nodes(const Lane&) const { return dag.nodes; }
     __device__ __forceinline__ const SubDag& subdag(const Lane&, uint32_t k) const { return dag.sd[k]; }
     __device__ __forceinline__ float4 ray_origin(const Lane&, uint64_t i) const { return __ldg(orig + i); }
@@ -124,7 +125,7 @@ __device__ __forceinline__ void lane_finish(Lane& L, const Src& c, bool hit, flo
         r.pz = __fadd_rn(L.o.z, __fmul_rn(L.d.z, dist));
     }
     r.status = L.status;
-    if ((c.q.flags & 1u) && r.hit && !(r.distance <= L.o.w)) {
+    if ((c.query(L).flags & 1u) && r.hit && !(r.distance <= L.o.w)) {
         r.hit = false;
         r.distance = 0.0f;
         r.material = 0u;
@@ -219,7 +220,7 @@ __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
         const float c0y = (L.fy - L.roy) * L.iy;
         const float c0z = (L.fz - L.roz) * L.iz;
         const float tce = max3_ref(c0x, c0y, c0z);
-        if (child >= kMaterialCount && large_footprint(L.cns, tcx, c.q.max_footprint)) {
+        if (child >= kMaterialCount && large_footprint(L.cns, tcx, c.query(L).max_footprint)) {
             if (tcx < L.last_exit) {
                 stack.put(L.h, L.node);
                 L.written |= 1u << L.h;
@@ -236,7 +237,7 @@ __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
         } else {
             uint32_t material = 0u;
             float nx = 0.0f, ny = 0.0f, nz = 0.0f;
-            if (c.q.compute_surface) {
+            if (c.query(L).compute_surface) {
                 material = nearest_material(c.nodes(L), child, L.sign, L.fetches, L.status);
                 if (L.status != kRayOk) {
                     lane_finish(L, c, false, 0.0f, 0u, 0.0f, 0.0f, 0.0f);

@@ -1,0 +1,460 @@
+// Request server: continuous batching of ray-query requests against
+// device-resident DAGs (cbq_server_*).
+//
+//  - submit() queues a request (host rays in, host hits out) and returns a
+//    ticket at once.
+//  - A scheduler thread admits queued requests in FIFO order while the device
+//    memory budget (a pool allocated once at creation) has room for their ray
+//    and hit buffers and a launch slot is free.  Each admitted group becomes one
+//    launch on the slot's stream: copies in, one persistent multi-volume
+//    traversal (one job per request, each with its own query), copies out.
+//    Groups are launched while earlier ones are still running, so requests that
+//    arrive during a launch overlap it on the device.
+//  - A completion thread waits for each launch's event, frees the requests'
+//    memory and slot, records latency (submit -> results in host memory) and
+//    wakes waiters.
+// Nothing on the device waits on the host: every launch finishes on its own,
+// and host waits are on CUDA events or condition variables.
+#include "cbq_batch.cuh"
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <vector>
+
+using namespace cbq;
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+constexpr uint64_t kAlign = 256;
+constexpr uint64_t kBytesPerRay = 16 + 16 + 12 + 12 + 12 + 4 + 4 + 1 + 1;  // rays in, all hit fields out
+
+uint64_t align_up(uint64_t v) { return (v + kAlign - 1) & ~(kAlign - 1); }
+
+uint64_t request_bytes(uint64_t n) { return align_up(n * kBytesPerRay + 8 * kAlign); }
+
+struct Request {
+    uint64_t ticket = 0;
+    cbq_request r{};
+    uint64_t bytes = 0;
+    uint64_t offset = 0;
+    Clock::time_point submitted;
+    cbq_status status = CBQ_OK;
+};
+
+// First-fit allocator over [0, size).
+class Pool {
+public:
+    void init(uint64_t size)
+    {
+        free_.clear();
+        if (size) free_[0] = size;
+    }
+    bool alloc(uint64_t bytes, uint64_t* off)
+    {
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second < bytes) continue;
+            *off = it->first;
+            const uint64_t rest = it->second - bytes, start = it->first + bytes;
+            free_.erase(it);
+            if (rest) free_[start] = rest;
+            return true;
+        }
+        return false;
+    }
+    void release(uint64_t off, uint64_t bytes)
+    {
+        auto it = free_.emplace(off, bytes).first;
+        auto next = std::next(it);
+        if (next != free_.end() && it->first + it->second == next->first) {
+            it->second += next->second;
+            free_.erase(next);
+        }
+        if (it != free_.begin()) {
+            auto prev = std::prev(it);
+            if (prev->first + prev->second == it->first) {
+                prev->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+
+private:
+    std::map<uint64_t, uint64_t> free_;
+};
+
+struct Slot {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    dev::JobDesc* h_table = nullptr;  // pinned
+    dev::JobDesc* d_table = nullptr;
+    uint64_t* d_counter = nullptr;
+    std::vector<Request*> reqs;
+};
+
+double percentile(std::vector<double> v, double p)
+{
+    if (v.empty()) return 0.0;
+    std::sort(v.begin(), v.end());
+    const double idx = p * (double)(v.size() - 1);
+    const size_t lo = (size_t)idx;
+    const size_t hi = std::min(lo + 1, v.size() - 1);
+    return v[lo] + (v[hi] - v[lo]) * (idx - (double)lo);
+}
+
+}  // namespace
+
+struct cbq_server {
+    cbq_server_config cfg{};
+    int device = 0;
+    char* d_pool = nullptr;
+    Pool pool;
+    std::vector<Slot> slots;
+    std::deque<int> free_slots;
+    std::deque<int> inflight;
+    std::deque<Request*> queue;
+    std::map<uint64_t, cbq_status> finished;   // completed tickets not yet waited for
+    std::map<uint64_t, int> live;              // tickets queued or in flight
+    std::mutex mu;
+    std::condition_variable cv_sched, cv_complete, cv_done;
+    bool stopping = false;
+    bool scheduler_done = false;
+    uint64_t next_ticket = 1;
+    uint64_t completions = 0;  // generation count, bumped per finished launch
+    std::thread scheduler, completer;
+    // statistics
+    std::vector<double> latencies_us;
+    uint64_t submitted = 0, completed = 0, rays_completed = 0, launches = 0, launched_requests = 0;
+    Clock::time_point first_submit, last_complete;
+    bool have_first = false;
+
+    void run_scheduler();
+    void run_completer();
+    cbq_status enqueue(Slot& s, const std::vector<Request*>& group);
+};
+
+cbq_status cbq_server::enqueue(Slot& s, const std::vector<Request*>& group)
+{
+    uint32_t njobs = 0;
+    uint64_t total = 0;
+    uint32_t rows = 1;
+    for (Request* rq : group) {
+        const uint64_t n = rq->r.ray_count;
+        char* p = d_pool + rq->offset;
+        float* o = (float*)p;
+        float* d = (float*)(p + n * 16);
+        char* h = p + n * 32;
+        dev::HitsOut out;
+        out.position = (float*)h; h += align_up(n * 12);
+        out.normal = (float*)h; h += align_up(n * 12);
+        out.voxel = (int32_t*)h; h += align_up(n * 12);
+        out.distance = (float*)h; h += align_up(n * 4);
+        out.material = (uint32_t*)h; h += align_up(n * 4);
+        out.hit = (uint8_t*)h; h += align_up(n);
+        out.status = (uint8_t*)h;
+        if (cudaMemcpyAsync(o, rq->r.host_origin_tmax, n * 16, cudaMemcpyHostToDevice, s.stream) != cudaSuccess ||
+            cudaMemcpyAsync(d, rq->r.host_direction, n * 16, cudaMemcpyHostToDevice, s.stream) != cudaSuccess)
+            return CBQ_ERR_CUDA;
+        dev::JobDesc jd;
+        std::memset(&jd, 0, sizeof(jd));
+        fill_job_volume(jd, rq->r.dag);
+        jd.orig = (const float4*)o;
+        jd.dir = (const float4*)d;
+        jd.out = out;
+        jd.count = n;
+        jd.q.compute_surface = rq->r.query.compute_surface;
+        jd.q.max_footprint = rq->r.query.max_footprint;
+        jd.q.flags = rq->r.query.flags;
+        if (!rq->r.dag->flat_ok) {  // coordinates beyond +-2^24: the nested kernel, launched on its own
+            cbq_rays rays{o, d};
+            cbq_hits hits{out.hit, out.distance, out.material, out.position, out.normal, out.voxel, out.status};
+            cbq_status st = cbq_intersect(rq->r.dag, &rays, n, &rq->r.query, &hits, (cbq_stream_t)s.stream);
+            if (st != CBQ_OK) return st;
+            continue;
+        }
+        jd.first = total;
+        s.h_table[njobs++] = jd;
+        total += n;
+        rows = std::max<uint32_t>(rows, (uint32_t)rq->r.dag->max_height);
+    }
+    if (njobs) {
+        if (cudaMemcpyAsync(s.d_table, s.h_table, njobs * sizeof(dev::JobDesc), cudaMemcpyHostToDevice, s.stream) !=
+            cudaSuccess)
+            return CBQ_ERR_CUDA;
+        cbq_status st = launch_batch_kernel(s.d_table, njobs, total, s.d_counter, cfg.block, cfg.refill_min, rows,
+                                            device, s.stream);
+        if (st != CBQ_OK) return st;
+    }
+    // Results back to the host.
+    for (Request* rq : group) {
+        const uint64_t n = rq->r.ray_count;
+        char* h = d_pool + rq->offset + n * 32;
+        const cbq_hits& hh = rq->r.host_hits;
+        struct Copy { void* dst; size_t bytes; };
+        const Copy copies[] = {{hh.position, n * 12}, {hh.normal, n * 12}, {hh.voxel, n * 12},
+                               {hh.distance, n * 4}, {hh.material, n * 4}, {hh.hit, n}, {hh.status, n}};
+        for (const Copy& c : copies) {
+            if (c.dst && cudaMemcpyAsync(c.dst, h, c.bytes, cudaMemcpyDeviceToHost, s.stream) != cudaSuccess)
+                return CBQ_ERR_CUDA;
+            h += align_up(c.bytes);
+        }
+    }
+    return cudaEventRecord(s.done, s.stream) == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
+}
+
+void cbq_server::run_scheduler()
+{
+    cudaSetDevice(device);
+    std::unique_lock<std::mutex> lk(mu);
+    for (;;) {
+        cv_sched.wait(lk, [&] { return (!queue.empty() && !free_slots.empty()) || (stopping && queue.empty()); });
+        if (queue.empty()) break;  // stopping, and nothing left to launch
+        std::vector<Request*> group;
+        uint64_t rays = 0;
+        while (!queue.empty() && group.size() < (size_t)cfg.max_batch_requests) {
+            Request* rq = queue.front();
+            if (!group.empty() && rays + rq->r.ray_count > cfg.max_batch_rays) break;
+            uint64_t off = 0;
+            if (!pool.alloc(rq->bytes, &off)) break;  // FIFO: wait for memory rather than skip ahead
+            rq->offset = off;
+            group.push_back(rq);
+            rays += rq->r.ray_count;
+            queue.pop_front();
+        }
+        if (group.empty()) {
+            const uint64_t gen = completions;
+            cv_sched.wait(lk, [&] { return completions != gen; });
+            continue;
+        }
+        const int si = free_slots.front();
+        free_slots.pop_front();
+        lk.unlock();
+        const cbq_status st = enqueue(slots[si], group);
+        if (st != CBQ_OK) {
+            cudaGetLastError();
+            for (Request* rq : group) rq->status = st;
+            cudaEventRecord(slots[si].done, slots[si].stream);
+        }
+        lk.lock();
+        slots[si].reqs = group;
+        inflight.push_back(si);
+        launches++;
+        launched_requests += group.size();
+        cv_complete.notify_one();
+    }
+    scheduler_done = true;
+    cv_complete.notify_all();
+}
+
+void cbq_server::run_completer()
+{
+    cudaSetDevice(device);
+    std::unique_lock<std::mutex> lk(mu);
+    for (;;) {
+        cv_complete.wait(lk, [&] { return !inflight.empty() || scheduler_done; });
+        if (inflight.empty()) break;  // scheduler finished and everything completed
+        const int si = inflight.front();
+        lk.unlock();
+        const bool ok = cudaEventSynchronize(slots[si].done) == cudaSuccess;
+        const Clock::time_point now = Clock::now();
+        lk.lock();
+        inflight.pop_front();
+        for (Request* rq : slots[si].reqs) {
+            if (!ok && rq->status == CBQ_OK) rq->status = CBQ_ERR_CUDA;
+            latencies_us.push_back(std::chrono::duration<double, std::micro>(now - rq->submitted).count());
+            pool.release(rq->offset, rq->bytes);
+            finished[rq->ticket] = rq->status;
+            live.erase(rq->ticket);
+            completed++;
+            rays_completed += rq->r.ray_count;
+            delete rq;
+        }
+        slots[si].reqs.clear();
+        free_slots.push_back(si);
+        last_complete = now;
+        completions++;
+        cv_done.notify_all();
+        cv_sched.notify_all();
+    }
+}
+
+extern "C" {
+
+cbq_status cbq_server_create(const cbq_server_config* cfg, cbq_server** out)
+{
+    if (!out) return CBQ_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    cbq_server* s = new (std::nothrow) cbq_server();
+    if (!s) return CBQ_ERR_OUT_OF_MEMORY;
+    cbq_server_config c{};
+    if (cfg) c = *cfg;
+    if (c.device_memory_budget == 0) c.device_memory_budget = 1ull << 30;
+    if (c.max_inflight_launches <= 0) c.max_inflight_launches = 4;
+    if (c.max_batch_requests <= 0) c.max_batch_requests = 256;
+    if (c.max_batch_rays == 0) c.max_batch_rays = 4ull << 20;
+    if (c.block <= 0) c.block = 128;
+    if (c.refill_min == 0) c.refill_min = 8;
+    if (c.block > 256 || (c.block % 32) || c.refill_min > 32 || c.max_inflight_launches > 64 ||
+        c.max_batch_requests > 65536) {
+        delete s;
+        return CBQ_ERR_INVALID_ARGUMENT;
+    }
+    s->cfg = c;
+    if (cudaGetDevice(&s->device) != cudaSuccess) { delete s; return CBQ_ERR_CUDA; }
+    if (cudaMalloc((void**)&s->d_pool, c.device_memory_budget) != cudaSuccess) {
+        cudaGetLastError();
+        delete s;
+        return CBQ_ERR_OUT_OF_MEMORY;
+    }
+    s->pool.init(c.device_memory_budget);
+    s->slots.resize(c.max_inflight_launches);
+    const size_t table = (size_t)c.max_batch_requests * sizeof(dev::JobDesc);
+    bool ok = true;
+    for (int i = 0; i < c.max_inflight_launches && ok; i++) {
+        Slot& sl = s->slots[i];
+        ok = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) == cudaSuccess &&
+             cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) == cudaSuccess &&
+             cudaMallocHost((void**)&sl.h_table, table) == cudaSuccess &&
+             cudaMalloc((void**)&sl.d_counter, 256 + table) == cudaSuccess;
+        if (ok) sl.d_table = (dev::JobDesc*)((char*)sl.d_counter + 256);
+        s->free_slots.push_back(i);
+    }
+    if (!ok) {
+        cudaGetLastError();
+        s->stopping = true;
+        s->scheduler_done = true;
+        cbq_server_destroy(s);
+        return CBQ_ERR_OUT_OF_MEMORY;
+    }
+    s->scheduler = std::thread([s] { s->run_scheduler(); });
+    s->completer = std::thread([s] { s->run_completer(); });
+    *out = s;
+    return CBQ_OK;
+}
+
+cbq_status cbq_server_submit(cbq_server* s, const cbq_request* r, uint64_t* ticket)
+{
+    if (!s || !r || !ticket || !r->dag) return CBQ_ERR_INVALID_ARGUMENT;
+    if (r->dag->device != s->device) return CBQ_ERR_INVALID_ARGUMENT;
+    if (r->ray_count > 0 && (!r->host_origin_tmax || !r->host_direction)) return CBQ_ERR_INVALID_ARGUMENT;
+    const uint64_t bytes = request_bytes(r->ray_count);
+    if (bytes > s->cfg.device_memory_budget) return CBQ_ERR_CAPACITY;
+    Request* rq = new (std::nothrow) Request();
+    if (!rq) return CBQ_ERR_OUT_OF_MEMORY;
+    rq->r = *r;
+    rq->bytes = bytes;
+    rq->submitted = Clock::now();
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->stopping) { delete rq; return CBQ_ERR_SHUTDOWN; }
+    rq->ticket = s->next_ticket++;
+    *ticket = rq->ticket;
+    s->submitted++;
+    if (!s->have_first) { s->first_submit = rq->submitted; s->have_first = true; }
+    if (r->ray_count == 0) {  // nothing to do
+        s->finished[rq->ticket] = CBQ_OK;
+        s->completed++;
+        delete rq;
+        s->cv_done.notify_all();
+        return CBQ_OK;
+    }
+    s->live[rq->ticket] = 1;
+    s->queue.push_back(rq);
+    s->cv_sched.notify_one();
+    return CBQ_OK;
+}
+
+cbq_status cbq_server_wait(cbq_server* s, uint64_t ticket, int64_t timeout_us)
+{
+    if (!s) return CBQ_ERR_INVALID_ARGUMENT;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto ready = [&] { return s->finished.count(ticket) != 0 || s->live.count(ticket) == 0; };
+    if (timeout_us < 0) {
+        s->cv_done.wait(lk, ready);
+    } else if (!s->cv_done.wait_for(lk, std::chrono::microseconds(timeout_us), ready)) {
+        return CBQ_ERR_TIMEOUT;
+    }
+    auto it = s->finished.find(ticket);
+    if (it == s->finished.end()) return CBQ_ERR_NOT_FOUND;
+    const cbq_status st = it->second;
+    s->finished.erase(it);
+    return st;
+}
+
+cbq_status cbq_server_poll(cbq_server* s, uint64_t ticket, int32_t* done)
+{
+    if (!s || !done) return CBQ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->finished.count(ticket)) { *done = 1; return CBQ_OK; }
+    if (s->live.count(ticket)) { *done = 0; return CBQ_OK; }
+    return CBQ_ERR_NOT_FOUND;
+}
+
+cbq_status cbq_server_get_stats(cbq_server* s, cbq_server_stats* out)
+{
+    if (!s || !out) return CBQ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(s->mu);
+    std::memset(out, 0, sizeof(*out));
+    out->submitted = s->submitted;
+    out->completed = s->completed;
+    out->rays_completed = s->rays_completed;
+    out->launches = s->launches;
+    out->mean_requests_per_launch = s->launches ? (double)s->launched_requests / (double)s->launches : 0.0;
+    out->latency_p50_us = percentile(s->latencies_us, 0.50);
+    out->latency_p99_us = percentile(s->latencies_us, 0.99);
+    out->latency_max_us = s->latencies_us.empty() ? 0.0 : *std::max_element(s->latencies_us.begin(), s->latencies_us.end());
+    double sum = 0;
+    for (double v : s->latencies_us) sum += v;
+    out->latency_mean_us = s->latencies_us.empty() ? 0.0 : sum / (double)s->latencies_us.size();
+    out->queued = s->queue.size();
+    out->inflight_launches = s->inflight.size();
+    if (s->have_first && s->completed)
+        out->busy_seconds = std::chrono::duration<double>(s->last_complete - s->first_submit).count();
+    return CBQ_OK;
+}
+
+cbq_status cbq_server_reset_stats(cbq_server* s)
+{
+    if (!s) return CBQ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->latencies_us.clear();
+    s->submitted = s->completed = s->rays_completed = s->launches = s->launched_requests = 0;
+    s->have_first = false;
+    return CBQ_OK;
+}
+
+cbq_status cbq_server_destroy(cbq_server* s)
+{
+    if (!s) return CBQ_ERR_INVALID_ARGUMENT;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stopping = true;
+    }
+    s->cv_sched.notify_all();
+    if (s->scheduler.joinable()) s->scheduler.join();  // drains the queue
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->scheduler_done = true;
+    }
+    s->cv_complete.notify_all();
+    if (s->completer.joinable()) s->completer.join();  // waits for launches in flight
+    for (Slot& sl : s->slots) {
+        if (sl.stream) cudaStreamDestroy(sl.stream);
+        if (sl.done) cudaEventDestroy(sl.done);
+        if (sl.h_table) cudaFreeHost(sl.h_table);
+        if (sl.d_counter) cudaFree(sl.d_counter);
+    }
+    if (s->d_pool) cudaFree(s->d_pool);
+    for (Request* rq : s->queue) delete rq;
+    delete s;
+    return CBQ_OK;
+}
+
+}  // extern "C"

@@ -123,6 +123,56 @@ def batch_volumes(count: int = 64, seed: int = 20240610, edge_log2=(7, 11), rays
     return out
 
 
+SERVE_EDGES_LOG2 = (10, 11, 12, 10, 11, 12, 11, 10)
+
+
+def serve_volumes(seed: int = 4242):
+    """The serving workload's 8 resident DAGs: seeded terrain scenes with edges
+    1024..4096."""
+    return [terrain_scaled(k, seed + i) for i, k in enumerate(SERVE_EDGES_LOG2)]
+
+
+def serve_ray_pools(scene: SceneSpec, collision: int, view_side: int, seed: int):
+    """Ray pools from which serving requests take contiguous slices:
+    collision rays from uniform points of the lower half of the volume (where
+    the terrain is) in uniform directions, with tmax uniform in [8, 64]
+    voxels; and unbounded view rays of a view_side^2 pinhole camera."""
+    import random
+
+    e = float(1 << scene.edge_log2)
+    co, cd = cbq.sphere_rays((0.0, 0.0, 0.0), (e, e, e / 2), collision, seed)
+    rng = random.Random(seed)
+    co[:, 3] = np.array([rng.uniform(8.0, 64.0) for _ in range(collision)], dtype=np.float32)
+    vo, vd = camera_scaled(scene.edge_log2, view_side, view_side).rays()
+    return (co, cd), (vo, vd)
+
+
+@dataclass(frozen=True)
+class ServeRequest:
+    volume: int          # index into serve_volumes()
+    collision: bool      # True: tmax-bounded collision rays; False: unbounded view rays
+    start: int           # slice start in the pool
+    count: int
+
+
+def serve_requests(count: int, pool_sizes: tuple, seed: int = 99, rays=(1024, 262144), collision_share=0.7,
+                   volumes: int = len(SERVE_EDGES_LOG2)):
+    """Request stream: sizes log-uniform in `rays`, 70% collision and 30% view
+    rays, volumes uniform.  pool_sizes = (collision pool size, view pool size)."""
+    import math
+    import random
+
+    rng = random.Random(seed)
+    out = []
+    for _ in range(count):
+        n = int(round(math.exp(rng.uniform(math.log(rays[0]), math.log(rays[1])))))
+        coll = rng.random() < collision_share
+        size = pool_sizes[0] if coll else pool_sizes[1]
+        n = min(n, size)
+        out.append(ServeRequest(rng.randrange(volumes), coll, rng.randrange(0, size - n + 1), n))
+    return out
+
+
 def bounce_from_hits(hits: dict, n: int, seed: int = TERRAIN_BOUNCE_SEED):
     """Bounce rays from the hits of a primary pass (host arrays or tensors)."""
     hit = _np(hits["hit"]).astype(bool)

@@ -233,6 +233,58 @@ cbq_status cbq_batch_destroy(cbq_batch* b);
 cbq_status cbq_intersect_batch(const cbq_job* jobs, int32_t job_count, const cbq_query* query,
                                cbq_stream_t stream);
 
+/* ------------------------------------------------------- serving */
+
+/* A request: host rays in, host hits out, against a resident DAG.  The host
+ * buffers must stay valid until the request has completed (cbq_server_wait). */
+typedef struct cbq_request {
+    const cbq_dag* dag;
+    const float* host_origin_tmax;  /* 4 floats per ray */
+    const float* host_direction;    /* 4 floats per ray */
+    uint64_t ray_count;
+    cbq_query query;                /* per request (e.g. CBQ_QUERY_TMAX for collision rays) */
+    cbq_hits host_hits;             /* host arrays; NULL fields are not copied back */
+} cbq_request;
+
+typedef struct cbq_server_config {
+    uint64_t device_memory_budget;  /* bytes for in-flight ray and hit buffers (0 = 1 GiB);
+                                       a request needs about 78 bytes per ray */
+    int32_t max_inflight_launches;  /* launches on the device at once (0 = 4) */
+    int32_t max_batch_requests;     /* requests per launch (0 = 256) */
+    uint64_t max_batch_rays;        /* rays per launch (0 = 4 Mi) */
+    int32_t block;                  /* threads per block (0 = 128) */
+    uint32_t refill_min;            /* idle lanes that trigger a refill (0 = 8) */
+} cbq_server_config;
+
+typedef struct cbq_server_stats {
+    uint64_t submitted, completed, rays_completed, launches;
+    uint64_t queued, inflight_launches;
+    double mean_requests_per_launch;
+    double latency_p50_us, latency_p99_us, latency_max_us, latency_mean_us; /* submit -> hits on host */
+    double busy_seconds;            /* first submit -> last completion */
+} cbq_server_stats;
+
+/* Continuous batching: requests are admitted in arrival order while the memory
+ * budget and a launch slot allow, grouped into one persistent multi-volume
+ * launch per group, and launched while earlier groups still run.  Each result
+ * equals cbq_intersect_host on that request alone. */
+typedef struct cbq_server cbq_server;
+
+cbq_status cbq_server_create(const cbq_server_config* cfg, cbq_server** out);
+/* Queues a request; returns at once with a ticket.  CBQ_ERR_CAPACITY if the
+ * request could never fit in the memory budget; CBQ_ERR_SHUTDOWN while the
+ * server is being destroyed. */
+cbq_status cbq_server_submit(cbq_server* s, const cbq_request* r, uint64_t* ticket);
+/* Waits for a ticket (timeout_us < 0: no limit) and returns the request's
+ * status; CBQ_ERR_TIMEOUT if it is still running, CBQ_ERR_NOT_FOUND for an
+ * unknown or already-waited ticket. */
+cbq_status cbq_server_wait(cbq_server* s, uint64_t ticket, int64_t timeout_us);
+cbq_status cbq_server_poll(cbq_server* s, uint64_t ticket, int32_t* done);
+cbq_status cbq_server_get_stats(cbq_server* s, cbq_server_stats* out);
+cbq_status cbq_server_reset_stats(cbq_server* s);
+/* Finishes every queued and running request, then stops. */
+cbq_status cbq_server_destroy(cbq_server* s);
+
 /* Statistics form of cbq_intersect: writes only the number of node fetches
  * (dependent child loads) each ray performed to the device array `fetches`. */
 cbq_status cbq_count_fetches(const cbq_dag* dag, const cbq_rays* rays, uint64_t n,

@@ -1,0 +1,133 @@
+"""The request server (cbq_server_*): continuous batching over resident DAGs.
+
+Each result must be the same alone (cbq_intersect_host on that request only)
+and in the mix (submitted together with many others, batched into shared
+launches, overlapping on the device)."""
+import threading
+
+import numpy as np
+import pytest
+
+import cubiquity_gb300 as cbq
+import oracle
+from cubiquity_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+FIELDS = ("hit", "distance", "material", "position", "normal", "voxel", "status")
+
+
+@pytest.fixture(scope="module")
+def served():
+    torch.cuda.set_device(0)
+    scenes = [W.terrain_scaled(k, 500 + i) for i, k in enumerate((6, 7, 8, 7))]
+    dags, pools = [], []
+    for i, s in enumerate(scenes):
+        nodes, root = s.build()
+        dags.append(cbq.Dag(nodes, root))
+        pools.append(W.serve_ray_pools(s, 40000, 128, 1000 + i))
+    return dags, pools
+
+
+def _query(collision):
+    return cbq.Query(True, cbq.MAX_FOOTPRINT_DISABLED, use_tmax=collision)
+
+
+def _same(a, b):
+    for k in FIELDS:
+        assert oracle.same_bits_nan_equal(a[k], b[k]), k
+
+
+def test_each_result_is_the_same_alone_and_in_the_mix(served):
+    dags, pools = served
+    reqs = W.serve_requests(60, (40000, 128 * 128), seed=7, rays=(1, 20000), volumes=len(dags))
+    server = cbq.Server(device_memory_budget=64 << 20, max_inflight_launches=3, max_batch_requests=16,
+                        max_batch_rays=50000)
+    tickets = []
+    for r in reqs:
+        (co, cd), (vo, vd) = pools[r.volume]
+        o, d = (co, cd) if r.collision else (vo, vd)
+        sl = slice(r.start, r.start + r.count)
+        t, out = server.submit(dags[r.volume], o[sl], d[sl], _query(r.collision))
+        tickets.append((t, out, r))
+    for t, out, r in tickets:
+        assert server.wait(t) == 0
+        (co, cd), (vo, vd) = pools[r.volume]
+        o, d = (co, cd) if r.collision else (vo, vd)
+        sl = slice(r.start, r.start + r.count)
+        alone = cbq.intersect_volume_host(dags[r.volume], o[sl], d[sl], use_tmax=r.collision)
+        _same(out, alone)
+    st = server.stats()
+    assert st["completed"] == len(reqs) and st["rays_completed"] == sum(r.count for r in reqs)
+    assert st["launches"] < len(reqs)  # requests shared launches
+    assert st["latency_p50_us"] > 0 and st["latency_p99_us"] >= st["latency_p50_us"]
+    server.close()
+
+
+def test_collision_rays_match_the_oracle(served, orc):
+    dags, pools = served
+    (co, cd), _ = pools[1]
+    nodes, root = W.terrain_scaled(7, 501).build()
+    server = cbq.Server(device_memory_budget=32 << 20)
+    t, out = server.submit(dags[1], co[:5000], cd[:5000], _query(True))
+    server.wait(t)
+    want = orc.intersect(nodes, orc.find_subdags(nodes, root), co[:5000], cd[:5000], use_tmax=True)
+    for k in FIELDS:
+        w = want[k]
+        assert oracle.same_bits_nan_equal(out[k].astype(w.dtype) if k == "material" else out[k], w), k
+    server.close()
+
+
+def test_submissions_from_several_threads(served):
+    dags, pools = served
+    server = cbq.Server(device_memory_budget=64 << 20, max_inflight_launches=4)
+    results = {}
+    errors = []
+
+    def worker(w):
+        try:
+            for k in range(10):
+                (co, cd), _ = pools[(w + k) % len(dags)]
+                sl = slice(1000 * k, 1000 * k + 777 + 100 * w)
+                t, out = server.submit(dags[(w + k) % len(dags)], co[sl], cd[sl], _query(True))
+                server.wait(t)
+                results[(w, k)] = (out, (w + k) % len(dags), sl)
+        except Exception as e:  # noqa: BLE001
+            errors.append(e)
+
+    th = [threading.Thread(target=worker, args=(w,)) for w in range(4)]
+    for x in th:
+        x.start()
+    for x in th:
+        x.join()
+    assert not errors
+    for (w, k), (out, v, sl) in results.items():
+        (co, cd), _ = pools[v]
+        _same(out, cbq.intersect_volume_host(dags[v], co[sl], cd[sl], use_tmax=True))
+    server.close()
+
+
+def test_admission_capacity_timeout_and_shutdown(served):
+    dags, pools = served
+    (co, cd), _ = pools[0]
+    server = cbq.Server(device_memory_budget=1 << 20)  # about 13k rays of buffers
+    with pytest.raises(cbq.CbqError) as e:
+        server.submit(dags[0], co[:20000], cd[:20000])
+    assert e.value.status == 10  # CBQ_ERR_CAPACITY: could never be admitted
+    # Requests that together exceed the budget are admitted one after another.
+    tickets = [server.submit(dags[0], co[i * 9000:(i + 1) * 9000], cd[i * 9000:(i + 1) * 9000])[0]
+               for i in range(4)]
+    for t in tickets:
+        assert server.wait(t) == 0
+    with pytest.raises(cbq.CbqError) as e:
+        server.wait(123456789)
+    assert e.value.status == 8  # unknown ticket
+    t0, _ = server.submit(dags[0], co[:0], cd[:0])  # empty request completes at once
+    assert server.wait(t0, 0) == 0
+    # Destroy with work queued: everything finishes first.
+    pending = [server.submit(dags[1], co[:5000], cd[:5000])[1] for _ in range(5)]
+    server.close()
+    want = cbq.intersect_volume_host(dags[1], co[:5000], cd[:5000])
+    for out in pending:
+        _same(out, want)
