@@ -17,7 +17,8 @@ CSRC = PKG_DIR / "csrc"
 BUILD_DIR = PKG_DIR / "_build"
 LIB_PATH = PKG_DIR / "libcbq.so"
 
-CUDA_SOURCES = ["cbq_api.cu", "cbq_flat.cu", "cbq_batch.cu", "cbq_server.cu", "cbq_probe.cu", "cbq_noalloc.cu"]
+CUDA_SOURCES = ["cbq_api.cu", "cbq_flat.cu", "cbq_batch.cu", "cbq_server.cu", "cbq_pathtrace.cu", "cbq_probe.cu",
+                "cbq_noalloc.cu"]
 CXX_SOURCES = ["cbq_host.cpp", "cbq_builder.cpp"]
 
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"

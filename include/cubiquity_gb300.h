@@ -285,6 +285,45 @@ cbq_status cbq_server_reset_stats(cbq_server* s);
 /* Finishes every queued and running request, then stops. */
 cbq_status cbq_server_destroy(cbq_server* s);
 
+/* ------------------------------------------------------- pathtracer */
+
+/* Wavefront restatement of the reference's CPU pathtracer
+ * (pathtracing_demo.cpp:81-190) on top of the traversal: per sample pass,
+ * camera rays, then for each depth an extension traversal (surface properties
+ * on), shading (material colour, emission, a sun and a sky shadow ray, a
+ * cosine bounce ray) and a shadow traversal (surface properties off), all with
+ * the LOD footprint `max_footprint`.  Counter-based random numbers (seed,
+ * pixel, sample, depth): a frame is reproducible. */
+typedef struct cbq_pt_material {
+    float albedo[3];
+    float emission[3];
+} cbq_pt_material;
+
+typedef struct cbq_pt_config {
+    int32_t width, height, samples_per_pixel, bounces;
+    double eye[3], target[3];
+    double tan_half_fov;
+    float max_footprint;            /* the demo uses 0.0035 (pathtracing_demo.h:84) */
+    float sun_direction[3], sun_colour[3], sky_colour[3], background[3];
+    uint64_t seed;
+    const cbq_pt_material* materials; /* 256 entries, host memory */
+} cbq_pt_config;
+
+typedef struct cbq_pt_stats {
+    uint64_t extension_rays, shadow_rays;
+    double milliseconds;
+} cbq_pt_stats;
+
+/* Called after every traversal wave with device pointers to its rays and hits
+ * (kind 0: extension rays, 1: shadow rays); the stream has been synchronised. */
+typedef void (*cbq_pt_wave_fn)(void* user, int32_t kind, int32_t depth, int32_t sample, const float* origin_tmax,
+                               const float* direction, uint64_t n, const cbq_hits* hits, const cbq_query* query);
+
+/* Renders into device_image (width * height * 3 floats, the mean over samples).
+ * Synchronous; allocates its wave buffers for the call. */
+cbq_status cbq_pathtrace(const cbq_dag* dag, const cbq_pt_config* cfg, float* device_image,
+                         cbq_pt_wave_fn on_wave, void* user, cbq_pt_stats* stats, cbq_stream_t stream);
+
 /* Statistics form of cbq_intersect: writes only the number of node fetches
  * (dependent child loads) each ray performed to the device array `fetches`. */
 cbq_status cbq_count_fetches(const cbq_dag* dag, const cbq_rays* rays, uint64_t n,
