@@ -563,6 +563,93 @@ class Server:
             pass
 
 
+# ------------------------------------------------------------ pathtracer
+
+class _PtMaterial(ctypes.Structure):
+    _fields_ = [("albedo", ctypes.c_float * 3), ("emission", ctypes.c_float * 3)]
+
+
+class _PtConfig(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("samples_per_pixel", ctypes.c_int32),
+                ("bounces", ctypes.c_int32), ("eye", ctypes.c_double * 3), ("target", ctypes.c_double * 3),
+                ("tan_half_fov", ctypes.c_double), ("max_footprint", ctypes.c_float),
+                ("sun_direction", ctypes.c_float * 3), ("sun_colour", ctypes.c_float * 3),
+                ("sky_colour", ctypes.c_float * 3), ("background", ctypes.c_float * 3), ("seed", ctypes.c_uint64),
+                ("materials", ctypes.POINTER(_PtMaterial))]
+
+
+class _PtStats(ctypes.Structure):
+    _fields_ = [("extension_rays", ctypes.c_uint64), ("shadow_rays", ctypes.c_uint64),
+                ("milliseconds", ctypes.c_double)]
+
+
+PT_WAVE_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
+                              ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(_Hits), ctypes.POINTER(_Query))
+_sig("cbq_pathtrace", [_P, ctypes.POINTER(_PtConfig), _P, PT_WAVE_FN, _P, ctypes.POINTER(_PtStats), _P])
+_sig("cbq_copy_to_host", [_P, _P, _U64])
+
+
+def copy_to_host(device_ptr: int, shape, dtype) -> np.ndarray:
+    """Copies a device buffer (a raw pointer) into a new numpy array."""
+    out = np.empty(shape, dtype=dtype)
+    _check(_lib.cbq_copy_to_host(_np_ptr(out), device_ptr, out.nbytes), "cbq_copy_to_host")
+    return out
+
+
+class WaveRecorder:
+    """A pathtracer on_wave callback that copies every wave's rays and hits to
+    the host: self.waves = [(kind, depth, sample, origin_tmax, direction, hits, query)]."""
+
+    def __init__(self):
+        self.waves = []
+
+    def __call__(self, kind, depth, sample, o_ptr, d_ptr, n, hits, query):
+        o = copy_to_host(o_ptr, (n, 4), np.float32)
+        d = copy_to_host(d_ptr, (n, 4), np.float32)
+        h = {"hit": copy_to_host(hits.hit, (n,), np.uint8)}
+        if hits.material:
+            h["material"] = copy_to_host(hits.material, (n,), np.uint32)
+        if hits.position:
+            h["position"] = copy_to_host(hits.position, (n, 3), np.float32)
+        if hits.normal:
+            h["normal"] = copy_to_host(hits.normal, (n, 3), np.float32)
+        self.waves.append((kind, depth, sample, o, d, h,
+                           (bool(query.compute_surface), float(query.max_footprint))))
+
+# The reference demo's lighting (pathtracing_demo.cpp:84-104, :131): sun along
+# normalize(1, -2, 10) with colour 0.1, sky colour 1.5, light-blue background.
+SUN_DIRECTION = tuple(float(v) for v in np.array([1.0, -2.0, 10.0]) / np.linalg.norm([1.0, -2.0, 10.0]))
+
+
+def pathtrace(dag: Dag, width: int, height: int, samples_per_pixel: int, bounces: int, eye, target,
+              materials: np.ndarray, tan_half_fov: float = 0.57735026918962576, max_footprint: float = 0.0035,
+              seed: int = 1, sun_direction=SUN_DIRECTION, sun_colour=(0.1, 0.1, 0.1), sky_colour=(1.5, 1.5, 1.5),
+              background=(0.8, 0.8, 1.0), on_wave=None, stream=None):
+    """Renders one frame; returns (image (height, width, 3) float32 CUDA tensor, stats dict).
+
+    materials: (256, 2, 3) array of (albedo, emission) per material.
+    on_wave(kind, depth, sample, origin_tmax_ptr, direction_ptr, n, hits, query) is called after
+    every traversal wave with device pointers (kind 0 extension, 1 shadow)."""
+    import torch
+    mats = np.ascontiguousarray(materials, dtype=np.float32).reshape(256, 2, 3)
+    arr = (_PtMaterial * 256)()
+    for m in range(256):
+        arr[m].albedo[:] = [float(v) for v in mats[m, 0]]
+        arr[m].emission[:] = [float(v) for v in mats[m, 1]]
+    cfg = _PtConfig(width, height, samples_per_pixel, bounces, (ctypes.c_double * 3)(*eye),
+                    (ctypes.c_double * 3)(*target), tan_half_fov, max_footprint, (ctypes.c_float * 3)(*sun_direction),
+                    (ctypes.c_float * 3)(*sun_colour), (ctypes.c_float * 3)(*sky_colour),
+                    (ctypes.c_float * 3)(*background), seed, arr)
+    image = torch.empty((height, width, 3), dtype=torch.float32, device="cuda")
+    stats = _PtStats()
+    cb = PT_WAVE_FN(lambda u, k, dp, s, o, d, n, h, q: on_wave(k, dp, s, o, d, n, h.contents, q.contents)) \
+        if on_wave else PT_WAVE_FN()
+    _check(_lib.cbq_pathtrace(dag.handle, ctypes.byref(cfg), image.data_ptr(), cb, None, ctypes.byref(stats),
+                              _stream_ptr(stream)), "cbq_pathtrace")
+    return image, {"extension_rays": stats.extension_rays, "shadow_rays": stats.shadow_rays,
+                   "milliseconds": stats.milliseconds}
+
+
 # ------------------------------------------------------------ batched form
 
 class Batch:

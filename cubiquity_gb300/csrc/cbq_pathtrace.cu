@@ -214,6 +214,13 @@ T* carve(char*& p, size_t count)
 
 }  // namespace
 
+extern "C" cbq_status cbq_copy_to_host(void* host_dst, const void* device_src, uint64_t bytes)
+{
+    if (bytes == 0) return CBQ_OK;
+    if (!host_dst || !device_src) return CBQ_ERR_INVALID_ARGUMENT;
+    return cudaMemcpy(host_dst, device_src, bytes, cudaMemcpyDeviceToHost) == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
+}
+
 extern "C" cbq_status cbq_pathtrace(const cbq_dag* dag, const cbq_pt_config* cfg, float* device_image,
                                     cbq_pt_wave_fn on_wave, void* user, cbq_pt_stats* stats, cbq_stream_t cstream)
 {

@@ -123,6 +123,32 @@ def batch_volumes(count: int = 64, seed: int = 20240610, edge_log2=(7, 11), rays
     return out
 
 
+CITY_8192 = SceneSpec(cbq.SCENE_CITY, 13, 8192001)
+CITY_EMISSIVE = (7, 23)  # the two emissive building materials
+
+
+def city_camera(edge_log2: int = 13):
+    """Eye and target of the city pathtracer view (z up), scaled to the edge."""
+    e = float(1 << edge_log2)
+    return (-0.15 * e, -0.2 * e, 0.45 * e), (0.55 * e, 0.5 * e, 0.0)
+
+
+def city_materials(seed: int = 77) -> np.ndarray:
+    """(256, 2, 3) albedo/emission: ground (1) grey, 32 building materials
+    (2..33) with seeded albedo in [0.2, 0.9], two of them emissive."""
+    import random
+
+    rng = random.Random(seed)
+    m = np.zeros((256, 2, 3), np.float32)
+    m[:, 0] = 0.5
+    m[1, 0] = (0.45, 0.45, 0.42)
+    for k in range(2, 34):
+        m[k, 0] = [rng.uniform(0.2, 0.9) for _ in range(3)]
+    for k in CITY_EMISSIVE:
+        m[k, 1] = (4.0, 3.4, 2.6)
+    return m
+
+
 SERVE_EDGES_LOG2 = (10, 11, 12, 10, 11, 12, 11, 10)
 
 

@@ -319,6 +319,10 @@ typedef struct cbq_pt_stats {
 typedef void (*cbq_pt_wave_fn)(void* user, int32_t kind, int32_t depth, int32_t sample, const float* origin_tmax,
                                const float* direction, uint64_t n, const cbq_hits* hits, const cbq_query* query);
 
+/* Convenience for wave callbacks in languages without a CUDA binding: a
+ * synchronous device-to-host copy. */
+cbq_status cbq_copy_to_host(void* host_dst, const void* device_src, uint64_t bytes);
+
 /* Renders into device_image (width * height * 3 floats, the mean over samples).
  * Synchronous; allocates its wave buffers for the call. */
 cbq_status cbq_pathtrace(const cbq_dag* dag, const cbq_pt_config* cfg, float* device_image,
