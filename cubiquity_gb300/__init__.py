@@ -68,13 +68,18 @@ class _Query(ctypes.Structure):
 KERNEL_AUTO, KERNEL_NESTED, KERNEL_FLAT = 0, 1, 2
 
 
+STACK_SHARED, STACK_LOCAL = 0, 1
+FORM_PLAIN, FORM_PERSISTENT, FORM_SORTED = 0, 1, 2
+
+
 class LaunchConfig(ctypes.Structure):
     """cbq_launch_config."""
     _fields_ = [("kernel", ctypes.c_int32), ("block", ctypes.c_int32), ("chunk", ctypes.c_uint32),
-                ("refill_min", ctypes.c_uint32)]
+                ("refill_min", ctypes.c_uint32), ("stack", ctypes.c_int32), ("form", ctypes.c_int32)]
 
     def as_dict(self):
-        return {"kernel": self.kernel, "block": self.block, "chunk": self.chunk, "refill_min": self.refill_min}
+        return {"kernel": self.kernel, "block": self.block, "chunk": self.chunk, "refill_min": self.refill_min,
+                "stack": self.stack, "form": self.form}
 
 
 class _DagInfo(ctypes.Structure):
@@ -121,6 +126,11 @@ _sig("cbq_intersect_host", [_P, _P, _P, _U64, ctypes.POINTER(_Query), ctypes.POI
 _sig("cbq_intersect_persistent", [_P, ctypes.POINTER(_Rays), _U64, ctypes.POINTER(_Query), ctypes.POINTER(_Hits),
                                   _P, _U32, _P])
 _sig("cbq_count_fetches", [_P, ctypes.POINTER(_Rays), _U64, ctypes.POINTER(_Query), _P, _P])
+_sig("cbq_scratch_bytes", [_U64], _U64)
+_sig("cbq_intersect_auto", [_P, ctypes.POINTER(_Rays), _U64, ctypes.POINTER(_Query), ctypes.POINTER(_Hits), _P, _U64,
+                            _P])
+_sig("cbq_autotune", [_P, ctypes.POINTER(_Rays), _U64, ctypes.POINTER(_Query), ctypes.POINTER(_Hits), _P, _U64,
+                      ctypes.c_int32, ctypes.POINTER(LaunchConfig), ctypes.POINTER(ctypes.c_float), _P])
 _sig("cbq_build_scene", [ctypes.c_int, ctypes.c_int, _U64, ctypes.c_int, ctypes.c_int,
                          ctypes.POINTER(ctypes.POINTER(ctypes.c_uint32)), ctypes.POINTER(_U64),
                          ctypes.POINTER(_U32)])
@@ -346,8 +356,8 @@ class Dag:
             pass
 
     def set_launch_config(self, kernel: int = KERNEL_AUTO, block: int = 0, chunk: int = 0,
-                          refill_min: int = 0) -> None:
-        cfg = LaunchConfig(kernel, block, chunk, refill_min)
+                          refill_min: int = 0, stack: int = STACK_SHARED, form: int = FORM_PERSISTENT) -> None:
+        cfg = LaunchConfig(kernel, block, chunk, refill_min, stack, form)
         _check(_lib.cbq_dag_set_launch_config(self.handle, ctypes.byref(cfg)), "cbq_dag_set_launch_config")
 
     def launch_config(self) -> dict:
@@ -429,6 +439,42 @@ def intersect_volume_persistent(dag: Dag, origin_tmax, direction, work_counter, 
                                          ctypes.byref(_hits_struct(out)), work_counter.data_ptr(), chunk,
                                          _stream_ptr(stream)), "cbq_intersect_persistent")
     return out
+
+
+def scratch_for(n: int, device="cuda"):
+    """Device scratch for intersect_auto / autotune over n rays (uint8 tensor)."""
+    import torch
+    return torch.empty(int(_lib.cbq_scratch_bytes(n)), dtype=torch.uint8, device=device)
+
+
+def intersect_auto(dag: Dag, origin_tmax, direction, scratch, compute_surface_properties=True,
+                   max_footprint=MAX_FOOTPRINT_DISABLED, use_tmax=False, out: dict | None = None, stream=None) -> dict:
+    """Traverses with the form and launch shape in the DAG's launch config
+    (plain, persistent or octant-sorted persistent), e.g. as set by autotune()."""
+    _check_rays_tensor(origin_tmax)
+    n = origin_tmax.shape[0]
+    _check_rays_tensor(direction, n)
+    if out is None:
+        out = alloc_hits(n, origin_tmax.device)
+    rays = _Rays(origin_tmax.data_ptr(), direction.data_ptr())
+    q = Query(compute_surface_properties, max_footprint, use_tmax).c()
+    _check(_lib.cbq_intersect_auto(dag.handle, ctypes.byref(rays), n, ctypes.byref(q), ctypes.byref(_hits_struct(out)),
+                                   scratch.data_ptr(), scratch.numel(), _stream_ptr(stream)), "cbq_intersect_auto")
+    return out
+
+
+def autotune_launch(dag: Dag, origin_tmax, direction, scratch, out: dict, compute_surface_properties=True,
+                    max_footprint=MAX_FOOTPRINT_DISABLED, use_tmax=False, repetitions: int = 3, stream=None):
+    """Runs the native autotuner on these rays; returns (config dict, ms per launch)."""
+    n = origin_tmax.shape[0]
+    rays = _Rays(origin_tmax.data_ptr(), direction.data_ptr())
+    q = Query(compute_surface_properties, max_footprint, use_tmax).c()
+    best = LaunchConfig()
+    ms = ctypes.c_float()
+    _check(_lib.cbq_autotune(dag.handle, ctypes.byref(rays), n, ctypes.byref(q), ctypes.byref(_hits_struct(out)),
+                             scratch.data_ptr(), scratch.numel(), repetitions, ctypes.byref(best), ctypes.byref(ms),
+                             _stream_ptr(stream)), "cbq_autotune")
+    return best.as_dict(), ms.value
 
 
 def count_fetches(dag: Dag, origin_tmax, direction, compute_surface_properties=True,

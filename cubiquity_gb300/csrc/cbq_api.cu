@@ -1,4 +1,5 @@
 // Device-side C ABI: DAG upload, traversal launches (plain and persistent).
+#include "cbq_flat.cuh"
 #include "cbq_internal.hpp"
 #include "cbq_traverse.cuh"
 
@@ -9,14 +10,6 @@
 #include <new>
 
 using namespace cbq;
-
-namespace cbq {
-bool float_positions_exact(const cbq_dag* dag);
-cbq_status launch_flat(const cbq_dag* dag, const dev::DagParams& dp, const dev::QueryParams& q,
-                       const dev::HitsOut& out, const float4* orig, const float4* dir, uint64_t n,
-                       uint32_t* fetch_out, bool persistent, uint64_t* counter, int block, uint32_t refill_min,
-                       cudaStream_t stream);
-}  // namespace cbq
 
 namespace {
 
@@ -29,6 +22,17 @@ bool use_flat(const cbq_dag* dag)
 }
 
 int flat_block(const cbq_dag* dag) { return dag->cfg.block > 0 ? dag->cfg.block : kFlatBlockDefault; }
+
+FlatLaunch flat_launch(const cbq_dag* dag, bool persistent, uint64_t* counter, uint32_t refill)
+{
+    FlatLaunch fl;
+    fl.persistent = persistent;
+    fl.counter = counter;
+    fl.block = flat_block(dag);
+    fl.refill_min = refill ? refill : (dag->cfg.refill_min ? dag->cfg.refill_min : kRefillDefault);
+    fl.local_stack = dag->cfg.stack == CBQ_STACK_LOCAL;
+    return fl;
+}
 
 constexpr int kPlainBlock = 128;
 constexpr int kPersistBlock = 256;
@@ -217,8 +221,8 @@ cbq_status cbq_intersect(const cbq_dag* dag, const cbq_rays* rays, uint64_t n, c
     if (st != CBQ_OK) return st;
     if (use_flat(dag))
         return launch_flat(dag, make_dag_params(dag), make_query(query), make_hits(hits),
-                           (const float4*)rays->origin_tmax, (const float4*)rays->direction, n, nullptr, false,
-                           nullptr, flat_block(dag), 0u, (cudaStream_t)stream);
+                           (const float4*)rays->origin_tmax, (const float4*)rays->direction, n, nullptr,
+                           flat_launch(dag, false, nullptr, 0u), (cudaStream_t)stream);
     const uint64_t blocks = (n + kPlainBlock - 1) / kPlainBlock;
     if (blocks > 0x7fffffffull) return CBQ_ERR_INVALID_ARGUMENT;
     cbq_k_intersect_plain<<<(unsigned)blocks, kPlainBlock, 0, (cudaStream_t)stream>>>(
@@ -233,8 +237,94 @@ cbq_status cbq_dag_set_launch_config(cbq_dag* dag, const cbq_launch_config* cfg)
     if (cfg->kernel < CBQ_KERNEL_AUTO || cfg->kernel > CBQ_KERNEL_FLAT) return CBQ_ERR_INVALID_ARGUMENT;
     if (cfg->block < 0 || cfg->block > 256 || (cfg->block % 32) != 0) return CBQ_ERR_INVALID_ARGUMENT;
     if (cfg->refill_min > 32) return CBQ_ERR_INVALID_ARGUMENT;
+    if (cfg->stack != CBQ_STACK_SHARED && cfg->stack != CBQ_STACK_LOCAL) return CBQ_ERR_INVALID_ARGUMENT;
+    if (cfg->form < CBQ_FORM_PLAIN || cfg->form > CBQ_FORM_SORTED) return CBQ_ERR_INVALID_ARGUMENT;
     dag->cfg = *cfg;
     return CBQ_OK;
+}
+
+uint64_t cbq_scratch_bytes(uint64_t n) { return 256 + 4 * n; }
+
+cbq_status cbq_intersect_auto(const cbq_dag* dag, const cbq_rays* rays, uint64_t n, const cbq_query* query,
+                              const cbq_hits* hits, void* scratch, uint64_t scratch_bytes, cbq_stream_t stream)
+{
+    if (!dag || !hits || !rays) return CBQ_ERR_INVALID_ARGUMENT;
+    if (n == 0) return CBQ_OK;
+    if (!scratch || scratch_bytes < cbq_scratch_bytes(n) || ((uintptr_t)scratch & 15u))
+        return CBQ_ERR_INVALID_ARGUMENT;
+    cbq_status st = check_rays(rays);
+    if (st != CBQ_OK) return st;
+    // Scratch: [0, 8) work counter | [64, 128) octant counts and cursors | [256, 256 + 4n) permutation
+    uint64_t* counter = (uint64_t*)scratch;
+    uint32_t* counts = (uint32_t*)((char*)scratch + 64);
+    uint32_t* perm = (uint32_t*)((char*)scratch + 256);
+    const int form = dag->cfg.form;
+    if (form == CBQ_FORM_PLAIN || !use_flat(dag)) {
+        if (form == CBQ_FORM_PLAIN) return cbq_intersect(dag, rays, n, query, hits, stream);
+        return cbq_intersect_persistent(dag, rays, n, query, hits, counter, 0u, stream);
+    }
+    FlatLaunch fl = flat_launch(dag, true, counter, 0u);
+    if (form == CBQ_FORM_SORTED) {
+        st = launch_octant_sort((const float4*)rays->direction, n, counts, perm, dag->device, (cudaStream_t)stream);
+        if (st != CBQ_OK) return st;
+        fl.perm = perm;
+    }
+    return launch_flat(dag, make_dag_params(dag), make_query(query), make_hits(hits),
+                       (const float4*)rays->origin_tmax, (const float4*)rays->direction, n, nullptr, fl,
+                       (cudaStream_t)stream);
+}
+
+cbq_status cbq_autotune(cbq_dag* dag, const cbq_rays* rays, uint64_t n, const cbq_query* query,
+                        const cbq_hits* hits, void* scratch, uint64_t scratch_bytes, int32_t repetitions,
+                        cbq_launch_config* best, float* best_ms, cbq_stream_t stream)
+{
+    if (!dag || repetitions <= 0 || n == 0) return CBQ_ERR_INVALID_ARGUMENT;
+    if (!scratch || scratch_bytes < cbq_scratch_bytes(n)) return CBQ_ERR_INVALID_ARGUMENT;
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return CBQ_ERR_CUDA;
+    const cbq_launch_config saved = dag->cfg;
+    cbq_launch_config winner = saved;
+    float win_ms = 1e30f;
+    cbq_status st = CBQ_OK;
+    static const int blocks[] = {64, 128, 256};
+    static const uint32_t refills[] = {4, 8, 16};
+    static const int stacks[] = {CBQ_STACK_SHARED, CBQ_STACK_LOCAL};
+    for (int form = CBQ_FORM_PLAIN; form <= CBQ_FORM_SORTED && st == CBQ_OK; form++) {
+        for (int blk : blocks) {
+            for (uint32_t rf : refills) {
+                if (form == CBQ_FORM_PLAIN && rf != refills[0]) continue;  // refill unused
+                for (int stk : stacks) {
+                    cbq_launch_config c = saved;
+                    c.kernel = dag->flat_ok ? CBQ_KERNEL_FLAT : CBQ_KERNEL_NESTED;
+                    c.block = dag->flat_ok ? blk : 0;
+                    c.refill_min = rf;
+                    c.stack = stk;
+                    c.form = form;
+                    dag->cfg = c;
+                    st = cbq_intersect_auto(dag, rays, n, query, hits, scratch, scratch_bytes, stream);  // warm-up
+                    if (st != CBQ_OK) break;
+                    cudaEventRecord(e0, (cudaStream_t)stream);
+                    for (int r = 0; r < repetitions && st == CBQ_OK; r++)
+                        st = cbq_intersect_auto(dag, rays, n, query, hits, scratch, scratch_bytes, stream);
+                    cudaEventRecord(e1, (cudaStream_t)stream);
+                    if (st != CBQ_OK || cudaEventSynchronize(e1) != cudaSuccess) { st = CBQ_ERR_CUDA; break; }
+                    float ms = 0;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    ms /= (float)repetitions;
+                    if (ms < win_ms) { win_ms = ms; winner = c; }
+                    if (!dag->flat_ok) break;  // the nested kernel has no stack choice
+                }
+                if (st != CBQ_OK) break;
+            }
+            if (st != CBQ_OK) break;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    dag->cfg = st == CBQ_OK ? winner : saved;
+    if (best) *best = dag->cfg;
+    if (best_ms) *best_ms = st == CBQ_OK ? win_ms : 0.0f;
+    return st;
 }
 
 cbq_status cbq_dag_get_launch_config(const cbq_dag* dag, cbq_launch_config* cfg)
@@ -260,7 +350,7 @@ cbq_status cbq_count_fetches(const cbq_dag* dag, const cbq_rays* rays, uint64_t 
     std::memset(&none, 0, sizeof(none));
     if (use_flat(dag))
         return launch_flat(dag, make_dag_params(dag), make_query(query), none, (const float4*)rays->origin_tmax,
-                           (const float4*)rays->direction, n, fetches, false, nullptr, flat_block(dag), 0u,
+                           (const float4*)rays->direction, n, fetches, flat_launch(dag, false, nullptr, 0u),
                            (cudaStream_t)stream);
     const uint64_t blocks = (n + kPlainBlock - 1) / kPlainBlock;
     cbq_k_intersect_plain<<<(unsigned)blocks, kPlainBlock, 0, (cudaStream_t)stream>>>(
@@ -278,13 +368,11 @@ cbq_status cbq_intersect_persistent(const cbq_dag* dag, const cbq_rays* rays, ui
     if (n == 0) return CBQ_OK;  // an empty batch may carry NULL buffers
     cbq_status st = check_rays(rays);
     if (st != CBQ_OK) return st;
-    if (use_flat(dag)) {
-        const uint32_t refill = chunk ? std::min<uint32_t>(chunk, 32u)
-                                      : (dag->cfg.refill_min ? dag->cfg.refill_min : kRefillDefault);
+    if (use_flat(dag))
         return launch_flat(dag, make_dag_params(dag), make_query(query), make_hits(hits),
-                           (const float4*)rays->origin_tmax, (const float4*)rays->direction, n, nullptr, true,
-                           work_counter, flat_block(dag), refill, (cudaStream_t)stream);
-    }
+                           (const float4*)rays->origin_tmax, (const float4*)rays->direction, n, nullptr,
+                           flat_launch(dag, true, work_counter, std::min<uint32_t>(chunk, 32u)),
+                           (cudaStream_t)stream);
     if (chunk == 0) chunk = dag->cfg.chunk ? dag->cfg.chunk : kDefaultChunk;
     const int stack_h = std::max(1, (int)dag->max_height);
     const size_t smem = (size_t)stack_h * kPersistBlock * sizeof(uint32_t);

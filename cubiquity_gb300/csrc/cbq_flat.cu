@@ -1,4 +1,5 @@
-// Kernels of the flat traversal (cbq_flat.cuh) and their launchers.
+// Kernels of the flat traversal (cbq_flat.cuh), the octant sort, and their
+// launchers.
 #include "cbq_flat.cuh"
 #include "cbq_internal.hpp"
 
@@ -15,14 +16,18 @@ constexpr unsigned kFull = 0xffffffffu;
 // PERSISTENT = true : an SM-sized grid; when at least `refill_min` lanes of a
 //                     warp are idle, the warp takes that many new rays from
 //                     `counter` with one atomic and the idle lanes start them.
-template <bool PERSISTENT>
+// SHARED: descent stack in shared memory (one column per thread) or in a
+//         per-thread local array.
+// SORTED: ray g of the launch is ray perm[g] of the input (octant order).
+template <bool PERSISTENT, bool SHARED, bool SORTED>
 __global__ void __launch_bounds__(256) cbq_k_flat(FlatCtx c, uint64_t n, unsigned long long* __restrict__ counter,
-                                                  uint32_t refill_min)
+                                                  uint32_t refill_min, const uint32_t* __restrict__ perm)
 {
     extern __shared__ uint32_t smem_stack[];
-    SharedStack stack;
-    stack.base = smem_stack + threadIdx.x;
-    stack.stride = blockDim.x;
+    SharedStack sstack;
+    sstack.base = smem_stack + threadIdx.x;
+    sstack.stride = blockDim.x;
+    LocalStack lstack;
     const unsigned lane = threadIdx.x & 31u;
     const uint32_t below = (1u << lane) - 1u;
 
@@ -31,7 +36,7 @@ __global__ void __launch_bounds__(256) cbq_k_flat(FlatCtx c, uint64_t n, unsigne
     bool more = PERSISTENT;  // warp-uniform: the queue may still hold rays
     if (!PERSISTENT) {
         const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-        if (i < n) lane_begin(L, c, i);
+        if (i < n) lane_begin(L, c, SORTED ? (uint64_t)__ldg(perm + i) : i);
     }
     for (;;) {
         if (PERSISTENT && more) {
@@ -44,7 +49,7 @@ __global__ void __launch_bounds__(256) cbq_k_flat(FlatCtx c, uint64_t n, unsigne
                 base = __shfl_sync(kFull, base, leader);
                 if (L.mode == kLaneIdle) {
                     const uint64_t i = base + __popc(idle & below);
-                    if (i < n) lane_begin(L, c, i);
+                    if (i < n) lane_begin(L, c, SORTED ? (uint64_t)__ldg(perm + i) : i);
                 }
                 if (base + cnt >= n) more = false;
             }
@@ -54,12 +59,65 @@ __global__ void __launch_bounds__(256) cbq_k_flat(FlatCtx c, uint64_t n, unsigne
             continue;
         }
         lane_settle(L, c);
-        if (L.mode == kLaneWalk) lane_walk(L, c, stack);
+        if (L.mode == kLaneWalk) {
+            if (SHARED)
+                lane_walk(L, c, sstack);
+            else
+                lane_walk(L, c, lstack);
+        }
     }
 }
 
-template __global__ void cbq_k_flat<false>(FlatCtx, uint64_t, unsigned long long*, uint32_t);
-template __global__ void cbq_k_flat<true>(FlatCtx, uint64_t, unsigned long long*, uint32_t);
+// Octant of a ray: its direction sign bits (raytracing.cpp:416-417).
+__device__ __forceinline__ uint32_t octant_of(float4 d)
+{
+    return (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+}
+
+// counts[8] += rays per octant.
+__global__ void __launch_bounds__(256) cbq_k_octant_count(const float4* __restrict__ dir, uint32_t n,
+                                                          uint32_t* __restrict__ counts)
+{
+    __shared__ uint32_t c[8];
+    if (threadIdx.x < 8) c[threadIdx.x] = 0;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        atomicAdd(&c[octant_of(__ldg(dir + i))], 1u);
+    __syncthreads();
+    if (threadIdx.x < 8 && c[threadIdx.x]) atomicAdd(&counts[threadIdx.x], c[threadIdx.x]);
+}
+
+// perm[start(octant) + k] = i: rays grouped by octant (order within a group
+// follows the atomics).  Every index i < n is written exactly once.
+__global__ void __launch_bounds__(256) cbq_k_octant_scatter(const float4* __restrict__ dir, uint32_t n,
+                                                            const uint32_t* __restrict__ counts,
+                                                            uint32_t* __restrict__ cursor, uint32_t* __restrict__ perm)
+{
+    __shared__ uint32_t start[8];
+    if (threadIdx.x == 0) {
+        uint32_t s = 0;
+        for (int b = 0; b < 8; b++) {
+            start[b] = s;
+            s += counts[b];
+        }
+    }
+    __syncthreads();
+    const unsigned lane = threadIdx.x & 31u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
+        const uint32_t i = i0 + threadIdx.x;
+        const bool valid = i < n;
+        const unsigned act = __ballot_sync(kFull, valid);
+        if (!valid) continue;
+        const uint32_t b = octant_of(__ldg(dir + i));
+        const unsigned grp = __match_any_sync(act, b);
+        const int leader = __ffs(grp) - 1;
+        uint32_t base = 0;
+        if ((int)lane == leader) base = atomicAdd(&cursor[b], (uint32_t)__popc(grp));
+        base = __shfl_sync(grp, base, leader);
+        perm[start[b] + base + __popc(grp & ((1u << lane) - 1u))] = i;
+    }
+}
 
 }  // namespace dev
 
@@ -80,10 +138,49 @@ bool float_positions_exact(const cbq_dag* dag)
     return true;
 }
 
+namespace {
+
+template <bool P, bool S, bool O>
+cbq_status launch_variant(const dev::FlatCtx& c, uint64_t n, const FlatLaunch& fl, int rows, cudaStream_t stream,
+                          int device)
+{
+    const size_t smem = S ? (size_t)rows * fl.block * sizeof(uint32_t) : 0;
+    if (!P) {
+        const uint64_t blocks = (n + fl.block - 1) / fl.block;
+        if (blocks > 0x7fffffffull) return CBQ_ERR_INVALID_ARGUMENT;
+        dev::cbq_k_flat<false, S, O><<<(unsigned)blocks, fl.block, smem, stream>>>(c, n, nullptr, 0u, fl.perm);
+    } else {
+        int sms = 0, per_sm = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return CBQ_ERR_CUDA;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::cbq_k_flat<true, S, O>, fl.block, smem) !=
+            cudaSuccess)
+            return CBQ_ERR_CUDA;
+        per_sm = std::max(per_sm, 1);
+        if (cudaMemsetAsync(fl.counter, 0, sizeof(uint64_t), stream) != cudaSuccess) return CBQ_ERR_CUDA;
+        dev::cbq_k_flat<true, S, O><<<sms * per_sm, fl.block, smem, stream>>>(
+            c, n, (unsigned long long*)fl.counter, fl.refill_min, fl.perm);
+    }
+    return cudaGetLastError() == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
+}
+
+}  // namespace
+
+cbq_status launch_octant_sort(const float4* dir, uint64_t n, uint32_t* counts16, uint32_t* perm, int device,
+                              cudaStream_t stream)
+{
+    if (n >= 0xffffffffull) return CBQ_ERR_INVALID_ARGUMENT;
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return CBQ_ERR_CUDA;
+    if (cudaMemsetAsync(counts16, 0, 16 * sizeof(uint32_t), stream) != cudaSuccess) return CBQ_ERR_CUDA;
+    const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, (uint64_t)sms * 8));
+    dev::cbq_k_octant_count<<<grid, 256, 0, stream>>>(dir, (uint32_t)n, counts16);
+    dev::cbq_k_octant_scatter<<<grid, 256, 0, stream>>>(dir, (uint32_t)n, counts16, counts16 + 8, perm);
+    return cudaGetLastError() == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
+}
+
 cbq_status launch_flat(const cbq_dag* dag, const dev::DagParams& dp, const dev::QueryParams& q,
                        const dev::HitsOut& out, const float4* orig, const float4* dir, uint64_t n,
-                       uint32_t* fetch_out, bool persistent, uint64_t* counter, int block, uint32_t refill_min,
-                       cudaStream_t stream)
+                       uint32_t* fetch_out, const FlatLaunch& fl, cudaStream_t stream)
 {
     dev::FlatCtx c;
     c.dag = dp;
@@ -92,25 +189,23 @@ cbq_status launch_flat(const cbq_dag* dag, const dev::DagParams& dp, const dev::
     c.orig = orig;
     c.dir = dir;
     c.fetch_out = fetch_out;
+    if (fl.persistent && !fl.counter) return CBQ_ERR_INVALID_ARGUMENT;
+    if (fl.perm && n >= 0xffffffffull) return CBQ_ERR_INVALID_ARGUMENT;
     const int rows = std::max(1, (int)dag->max_height);
-    const size_t smem = (size_t)rows * block * sizeof(uint32_t);
-    if (!persistent) {
-        const uint64_t blocks = (n + block - 1) / block;
-        if (blocks > 0x7fffffffull) return CBQ_ERR_INVALID_ARGUMENT;
-        dev::cbq_k_flat<false><<<(unsigned)blocks, block, smem, stream>>>(c, n, nullptr, 0u);
-    } else {
-        if (!counter) return CBQ_ERR_INVALID_ARGUMENT;
-        int sms = 0, per_sm = 0;
-        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dag->device) != cudaSuccess)
-            return CBQ_ERR_CUDA;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::cbq_k_flat<true>, block, smem) != cudaSuccess)
-            return CBQ_ERR_CUDA;
-        per_sm = std::max(per_sm, 1);
-        if (cudaMemsetAsync(counter, 0, sizeof(uint64_t), stream) != cudaSuccess) return CBQ_ERR_CUDA;
-        dev::cbq_k_flat<true><<<sms * per_sm, block, smem, stream>>>(c, n, (unsigned long long*)counter,
-                                                                     refill_min);
+    const int dv = dag->device;
+    const bool sorted = fl.perm != nullptr;
+    if (fl.persistent) {
+        if (fl.local_stack)
+            return sorted ? launch_variant<true, false, true>(c, n, fl, rows, stream, dv)
+                          : launch_variant<true, false, false>(c, n, fl, rows, stream, dv);
+        return sorted ? launch_variant<true, true, true>(c, n, fl, rows, stream, dv)
+                      : launch_variant<true, true, false>(c, n, fl, rows, stream, dv);
     }
-    return cudaGetLastError() == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
+    if (fl.local_stack)
+        return sorted ? launch_variant<false, false, true>(c, n, fl, rows, stream, dv)
+                      : launch_variant<false, false, false>(c, n, fl, rows, stream, dv);
+    return sorted ? launch_variant<false, true, true>(c, n, fl, rows, stream, dv)
+                  : launch_variant<false, true, false>(c, n, fl, rows, stream, dv);
 }
 
 }  // namespace cbq

@@ -17,6 +17,7 @@
 // coordinates lie within +-2^24, where (float)(a + b) == (float)a + (float)b.
 #pragma once
 
+#include "../../include/cubiquity_gb300.h"
 #include "cbq_traverse.cuh"
 
 namespace cbq {
@@ -301,4 +302,27 @@ __device__ __forceinline__ void lane_settle(Lane& L, const Src& c)
 }
 
 }  // namespace dev
+
+// Launch shape of the single-volume flat kernel.
+struct FlatLaunch {
+    bool persistent = false;
+    uint64_t* counter = nullptr;     // persistent: work counter (zeroed by the launch)
+    int block = 64;
+    uint32_t refill_min = 8;
+    bool local_stack = false;        // descent stack in local memory instead of shared
+    const uint32_t* perm = nullptr;  // octant-sorted order (from launch_octant_sort), or null
+};
+
+}  // namespace cbq
+
+struct cbq_dag;
+namespace cbq {
+cbq_status launch_flat(const cbq_dag* dag, const dev::DagParams& dp, const dev::QueryParams& q,
+                       const dev::HitsOut& out, const float4* orig, const float4* dir, uint64_t n,
+                       uint32_t* fetch_out, const FlatLaunch& fl, cudaStream_t stream);
+// Groups ray indices by octant (direction sign bits) into perm[n]; counts16 is
+// 16 uint32 of scratch (zeroed here).
+cbq_status launch_octant_sort(const float4* dir, uint64_t n, uint32_t* counts16, uint32_t* perm, int device,
+                              cudaStream_t stream);
+bool float_positions_exact(const cbq_dag* dag);
 }  // namespace cbq

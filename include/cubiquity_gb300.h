@@ -140,15 +140,41 @@ typedef enum cbq_kernel {
     CBQ_KERNEL_FLAT = 2
 } cbq_kernel;
 
+#define CBQ_STACK_SHARED 0    /* descent stack in shared memory, one column per thread */
+#define CBQ_STACK_LOCAL 1     /* descent stack in a per-thread local array (L1) */
+
+#define CBQ_FORM_PLAIN 0      /* cbq_intersect_auto: one thread per ray */
+#define CBQ_FORM_PERSISTENT 1 /* persistent grid refilling idle lanes */
+#define CBQ_FORM_SORTED 2     /* rays grouped by octant first, then persistent */
+
 typedef struct cbq_launch_config {
     int32_t kernel;           /* cbq_kernel */
     int32_t block;            /* threads per block (multiple of 32, <= 256), 0 = default */
     uint32_t chunk;           /* nested persistent: rays per warp grab, 0 = default */
     uint32_t refill_min;      /* flat persistent: idle lanes that trigger a refill, 0 = default */
+    int32_t stack;            /* CBQ_STACK_* (flat kernel) */
+    int32_t form;             /* CBQ_FORM_*, used by cbq_intersect_auto */
 } cbq_launch_config;
 
 cbq_status cbq_dag_set_launch_config(cbq_dag* dag, const cbq_launch_config* cfg);
 cbq_status cbq_dag_get_launch_config(const cbq_dag* dag, cbq_launch_config* cfg);
+
+/* Device scratch cbq_intersect_auto needs for n rays (work counter, octant
+ * histogram and, for the sorted form, a uint32 permutation): 256 + 4n bytes. */
+uint64_t cbq_scratch_bytes(uint64_t n);
+
+/* Traverses with the form and launch shape in the DAG's launch config
+ * (CBQ_FORM_*), using caller-owned device scratch of cbq_scratch_bytes(n)
+ * bytes.  Results equal cbq_intersect's for every form. */
+cbq_status cbq_intersect_auto(const cbq_dag* dag, const cbq_rays* rays, uint64_t n, const cbq_query* query,
+                              const cbq_hits* hits, void* scratch, uint64_t scratch_bytes, cbq_stream_t stream);
+
+/* Autotuner: times every form x block {64,128,256} x refill {4,8,16} x stack
+ * {shared, local} on these rays (synchronous; `repetitions` launches each),
+ * stores the fastest in the DAG's launch config and returns it with its time. */
+cbq_status cbq_autotune(cbq_dag* dag, const cbq_rays* rays, uint64_t n, const cbq_query* query,
+                        const cbq_hits* hits, void* scratch, uint64_t scratch_bytes, int32_t repetitions,
+                        cbq_launch_config* best, float* best_ms, cbq_stream_t stream);
 
 /* Sets a persisting-L2 access-policy window over the node store on `stream`
  * (fraction of the device's persisting-L2 limit to reserve, 0 disables). */
