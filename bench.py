@@ -53,8 +53,9 @@ def parse_args():
     p.add_argument("--workload", choices=["terrain-4096", "spheres-256", "batch-64", "serve-8", "city-8192"],
                    default="terrain-4096")
     p.add_argument("--kernel", choices=["auto", "flat", "nested"], default="auto")
-    p.add_argument("--form", choices=["persistent", "plain"], default="persistent",
-                   help="persistent grid pulling rays from a work counter, or one thread per ray")
+    p.add_argument("--form", choices=["tuned", "persistent", "plain"], default="tuned",
+                   help="tuned: the autotuner's choice per batch (form, block, refill, stack); persistent: grid "
+                        "pulling rays from a work counter; plain: one thread per ray")
     p.add_argument("--block", type=int, default=0)
     p.add_argument("--chunk", type=int, default=0, help="persistent: refill threshold (flat) / grab size (nested)")
     p.add_argument("--e2e-steps", type=int, default=5)
@@ -294,9 +295,20 @@ def run_gpu(args, world, rank, local):
         dev_batches.append((label, to, td, out, f))
     counter = torch.zeros(1, dtype=torch.int64, device="cuda")
     rays_per_step = sum(b[1].shape[0] for b in dev_batches)
+    tuned = {}
+    if args.form == "tuned":
+        from cubiquity_gb300 import autotune
+        scratch = cbq.scratch_for(max(b[1].shape[0] for b in dev_batches))
+        for label, to, td, out, _ in dev_batches:
+            tuned[label] = autotune.tune(dag, to, td, scratch, out, stream=stream)
+        torch.cuda.synchronize()
 
     def launch(label, to, td, out):
-        if args.persistent:
+        if tuned:
+            c = tuned[label]
+            dag.set_launch_config(c["kernel"], c["block"], c["chunk"], c["refill_min"], c["stack"], c["form"])
+            cbq.intersect_auto(dag, to, td, scratch, out=out, stream=stream)
+        elif args.persistent:
             cbq.intersect_volume_persistent(dag, to, td, counter, chunk=args.chunk, out=out, stream=stream)
         else:
             cbq.intersect_volume(dag, to, td, out=out, stream=stream)
@@ -396,7 +408,7 @@ def run_gpu(args, world, rank, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded scene built by libcbq, generated rays)",
         "config": {"workload": args.workload, "rays_per_step": rays_per_step, "kernel": kernel_name,
-                   "persistent": bool(args.persistent), "launch_config": cfg,
+                   "form": args.form, "launch_config": tuned if tuned else cfg,
                    "batches": {b[0]: int(b[1].shape[0]) for b in dev_batches},
                    "dag_nodes": int(dag.node_count), "dag_bytes": int(dag.bytes),
                    "l2": "inputs larger than L2 (rays + hits %.0f MB per step); DAG read through L2"

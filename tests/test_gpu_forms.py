@@ -1,0 +1,80 @@
+"""Launch forms and the autotuner: every form (plain, persistent, octant-sorted
+persistent) x stack placement x block size gives the same bits as the plain
+drop-in; the autotuner picks one of them and its cache re-applies it."""
+import numpy as np
+import pytest
+
+import cubiquity_gb300 as cbq
+import oracle
+from cubiquity_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+FIELDS = ("hit", "distance", "material", "position", "normal", "voxel", "status")
+
+
+@pytest.fixture(scope="module")
+def scene():
+    torch.cuda.set_device(0)
+    spec = W.terrain_scaled(10, 424242)
+    nodes, root = spec.build()
+    dag = cbq.Dag(nodes, root)
+    o, d = W.camera_scaled(10, 384, 256).rays()
+    prim = cbq.intersect_volume(dag, torch.from_numpy(o).cuda(), torch.from_numpy(d).cuda())
+    bo, bd = W.bounce_from_hits({k: v.cpu().numpy() for k, v in prim.items()}, o.shape[0])
+    rays = {"primary": (torch.from_numpy(o).cuda(), torch.from_numpy(d).cuda()),
+            "bounce": (torch.from_numpy(bo).cuda(), torch.from_numpy(bd).cuda())}
+    return dag, rays
+
+
+def _same(a, b):
+    for k in FIELDS:
+        assert oracle.same_bits_nan_equal(a[k].cpu().numpy(), b[k].cpu().numpy()), k
+
+
+@pytest.mark.parametrize("form", [cbq.FORM_PLAIN, cbq.FORM_PERSISTENT, cbq.FORM_SORTED])
+@pytest.mark.parametrize("stack", [cbq.STACK_SHARED, cbq.STACK_LOCAL])
+@pytest.mark.parametrize("block", [64, 256])
+def test_every_form_equals_the_drop_in(scene, form, stack, block):
+    dag, rays = scene
+    scratch = cbq.scratch_for(max(o.shape[0] for o, _ in rays.values()))
+    for label, (o, d) in rays.items():
+        dag.set_launch_config(cbq.KERNEL_FLAT, 64, 0, 0, cbq.STACK_SHARED, cbq.FORM_PLAIN)
+        want = cbq.intersect_volume(dag, o, d)
+        dag.set_launch_config(cbq.KERNEL_FLAT, block, 0, 4, stack, form)
+        got = cbq.intersect_auto(dag, o, d, scratch)
+        _same(got, want)
+    dag.set_launch_config()
+
+
+def test_autotune_and_cache(scene, tmp_path, monkeypatch):
+    from cubiquity_gb300 import autotune
+    monkeypatch.setattr(autotune, "CACHE_PATH", tmp_path / "tune.json")
+    dag, rays = scene
+    o, d = rays["bounce"]
+    scratch = cbq.scratch_for(o.shape[0])
+    out = cbq.alloc_hits(o.shape[0])
+    first = autotune.tune(dag, o, d, scratch, out, repetitions=1)
+    assert not first["cached"] and first["form"] in (0, 1, 2) and first["stack"] in (0, 1)
+    assert first["block"] in (64, 128, 256) and first["ms"] > 0
+    dag.set_launch_config()
+    second = autotune.tune(dag, o, d, scratch, out)
+    assert second["cached"] and second["key"] == first["key"]
+    cfg = dag.launch_config()
+    assert (cfg["form"], cfg["block"], cfg["stack"]) == (first["form"], first["block"], first["stack"])
+    got = cbq.intersect_auto(dag, o, d, scratch)
+    dag.set_launch_config(cbq.KERNEL_FLAT, 64, 0, 0, cbq.STACK_SHARED, cbq.FORM_PLAIN)
+    _same(got, cbq.intersect_volume(dag, o, d))
+    dag.set_launch_config()
+    assert autotune.ray_mix(rays["primary"][1]) == "coherent"
+    assert autotune.ray_mix(o.new_tensor(np.random.default_rng(0).normal(size=(5000, 4)).astype(np.float32))) == \
+        "incoherent"
+
+
+def test_scratch_checks(scene):
+    dag, rays = scene
+    o, d = rays["primary"]
+    small = cbq.scratch_for(10)
+    with pytest.raises(cbq.CbqError):
+        cbq.intersect_auto(dag, o, d, small)
