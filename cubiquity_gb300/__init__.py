@@ -75,11 +75,12 @@ FORM_PLAIN, FORM_PERSISTENT, FORM_SORTED = 0, 1, 2
 class LaunchConfig(ctypes.Structure):
     """cbq_launch_config."""
     _fields_ = [("kernel", ctypes.c_int32), ("block", ctypes.c_int32), ("chunk", ctypes.c_uint32),
-                ("refill_min", ctypes.c_uint32), ("stack", ctypes.c_int32), ("form", ctypes.c_int32)]
+                ("refill_min", ctypes.c_uint32), ("stack", ctypes.c_int32), ("form", ctypes.c_int32),
+                ("steps", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
     def as_dict(self):
         return {"kernel": self.kernel, "block": self.block, "chunk": self.chunk, "refill_min": self.refill_min,
-                "stack": self.stack, "form": self.form}
+                "stack": self.stack, "form": self.form, "steps": self.steps}
 
 
 class _DagInfo(ctypes.Structure):
@@ -356,8 +357,9 @@ class Dag:
             pass
 
     def set_launch_config(self, kernel: int = KERNEL_AUTO, block: int = 0, chunk: int = 0,
-                          refill_min: int = 0, stack: int = STACK_SHARED, form: int = FORM_PERSISTENT) -> None:
-        cfg = LaunchConfig(kernel, block, chunk, refill_min, stack, form)
+                          refill_min: int = 0, stack: int = STACK_SHARED, form: int = FORM_PERSISTENT,
+                          steps: int = 1) -> None:
+        cfg = LaunchConfig(kernel, block, chunk, refill_min, stack, form, steps, 0)
         _check(_lib.cbq_dag_set_launch_config(self.handle, ctypes.byref(cfg)), "cbq_dag_set_launch_config")
 
     def launch_config(self) -> dict:

@@ -65,8 +65,10 @@ def tune(dag: cbq.Dag, origin_tmax, direction, scratch, out: dict, compute_surfa
     key = cache_key(dag, direction)
     cache = _load() if use_cache else {}
     if key in cache:
-        cfg = cache[key]["config"]
-        dag.set_launch_config(cfg["kernel"], cfg["block"], cfg["chunk"], cfg["refill_min"], cfg["stack"], cfg["form"])
+        cfg = dict(cache[key]["config"])
+        cfg.setdefault("steps", 1)
+        dag.set_launch_config(cfg["kernel"], cfg["block"], cfg["chunk"], cfg["refill_min"], cfg["stack"], cfg["form"],
+                              cfg["steps"])
         return dict(cfg, cached=True, key=key)
     cfg, ms = cbq.autotune_launch(dag, origin_tmax, direction, scratch, out, compute_surface_properties,
                                   max_footprint, use_tmax, repetitions, stream)

@@ -31,6 +31,7 @@ FlatLaunch flat_launch(const cbq_dag* dag, bool persistent, uint64_t* counter, u
     fl.block = flat_block(dag);
     fl.refill_min = refill ? refill : (dag->cfg.refill_min ? dag->cfg.refill_min : kRefillDefault);
     fl.local_stack = dag->cfg.stack == CBQ_STACK_LOCAL;
+    fl.steps = dag->cfg.steps > 0 ? (uint32_t)dag->cfg.steps : 1u;
     return fl;
 }
 
@@ -239,6 +240,7 @@ cbq_status cbq_dag_set_launch_config(cbq_dag* dag, const cbq_launch_config* cfg)
     if (cfg->refill_min > 32) return CBQ_ERR_INVALID_ARGUMENT;
     if (cfg->stack != CBQ_STACK_SHARED && cfg->stack != CBQ_STACK_LOCAL) return CBQ_ERR_INVALID_ARGUMENT;
     if (cfg->form < CBQ_FORM_PLAIN || cfg->form > CBQ_FORM_SORTED) return CBQ_ERR_INVALID_ARGUMENT;
+    if (cfg->steps < 0 || cfg->steps > 8) return CBQ_ERR_INVALID_ARGUMENT;
     dag->cfg = *cfg;
     return CBQ_OK;
 }
@@ -289,17 +291,20 @@ cbq_status cbq_autotune(cbq_dag* dag, const cbq_rays* rays, uint64_t n, const cb
     static const int blocks[] = {64, 128, 256};
     static const uint32_t refills[] = {4, 8, 16};
     static const int stacks[] = {CBQ_STACK_SHARED, CBQ_STACK_LOCAL};
+    static const int step_counts[] = {1, 2};
     for (int form = CBQ_FORM_PLAIN; form <= CBQ_FORM_SORTED && st == CBQ_OK; form++) {
         for (int blk : blocks) {
             for (uint32_t rf : refills) {
                 if (form == CBQ_FORM_PLAIN && rf != refills[0]) continue;  // refill unused
-                for (int stk : stacks) {
+                for (int stk_steps = 0; stk_steps < 4; stk_steps++) {
+                    const int stk = stacks[stk_steps & 1];
                     cbq_launch_config c = saved;
                     c.kernel = dag->flat_ok ? CBQ_KERNEL_FLAT : CBQ_KERNEL_NESTED;
                     c.block = dag->flat_ok ? blk : 0;
                     c.refill_min = rf;
                     c.stack = stk;
                     c.form = form;
+                    c.steps = step_counts[stk_steps >> 1];
                     dag->cfg = c;
                     st = cbq_intersect_auto(dag, rays, n, query, hits, scratch, scratch_bytes, stream);  // warm-up
                     if (st != CBQ_OK) break;

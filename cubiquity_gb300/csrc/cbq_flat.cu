@@ -21,7 +21,8 @@ constexpr unsigned kFull = 0xffffffffu;
 // SORTED: ray g of the launch is ray perm[g] of the input (octant order).
 template <bool PERSISTENT, bool SHARED, bool SORTED>
 __global__ void __launch_bounds__(256) cbq_k_flat(FlatCtx c, uint64_t n, unsigned long long* __restrict__ counter,
-                                                  uint32_t refill_min, const uint32_t* __restrict__ perm)
+                                                  uint32_t refill_min, const uint32_t* __restrict__ perm,
+                                                  uint32_t steps)
 {
     extern __shared__ uint32_t smem_stack[];
     SharedStack sstack;
@@ -59,7 +60,9 @@ __global__ void __launch_bounds__(256) cbq_k_flat(FlatCtx c, uint64_t n, unsigne
             continue;
         }
         lane_settle(L, c);
-        if (L.mode == kLaneWalk) {
+        // Up to `steps` ESVO steps per outer iteration: amortises the refill
+        // ballot and the settle check over several node fetches.
+        for (uint32_t k = 0; k < steps && L.mode == kLaneWalk; k++) {
             if (SHARED)
                 lane_walk(L, c, sstack);
             else
@@ -148,7 +151,8 @@ cbq_status launch_variant(const dev::FlatCtx& c, uint64_t n, const FlatLaunch& f
     if (!P) {
         const uint64_t blocks = (n + fl.block - 1) / fl.block;
         if (blocks > 0x7fffffffull) return CBQ_ERR_INVALID_ARGUMENT;
-        dev::cbq_k_flat<false, S, O><<<(unsigned)blocks, fl.block, smem, stream>>>(c, n, nullptr, 0u, fl.perm);
+        dev::cbq_k_flat<false, S, O><<<(unsigned)blocks, fl.block, smem, stream>>>(c, n, nullptr, 0u, fl.perm,
+                                                                                     fl.steps ? fl.steps : 1u);
     } else {
         int sms = 0, per_sm = 0;
         if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return CBQ_ERR_CUDA;
@@ -158,7 +162,7 @@ cbq_status launch_variant(const dev::FlatCtx& c, uint64_t n, const FlatLaunch& f
         per_sm = std::max(per_sm, 1);
         if (cudaMemsetAsync(fl.counter, 0, sizeof(uint64_t), stream) != cudaSuccess) return CBQ_ERR_CUDA;
         dev::cbq_k_flat<true, S, O><<<sms * per_sm, fl.block, smem, stream>>>(
-            c, n, (unsigned long long*)fl.counter, fl.refill_min, fl.perm);
+            c, n, (unsigned long long*)fl.counter, fl.refill_min, fl.perm, fl.steps ? fl.steps : 1u);
     }
     return cudaGetLastError() == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
 }

@@ -311,6 +311,7 @@ struct FlatLaunch {
     uint32_t refill_min = 8;
     bool local_stack = false;        // descent stack in local memory instead of shared
     const uint32_t* perm = nullptr;  // octant-sorted order (from launch_octant_sort), or null
+    uint32_t steps = 1;              // ESVO steps per outer loop iteration
 };
 
 }  // namespace cbq

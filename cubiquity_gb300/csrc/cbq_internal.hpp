@@ -31,7 +31,7 @@ struct cbq_dag {
     int32_t max_height = 0;        // max SubDAG height (stack depth)
     int device = 0;
     bool flat_ok = false;          // float positions exact (coordinates within +-2^24)
-    cbq_launch_config cfg{CBQ_KERNEL_AUTO, 0, 0, 0, CBQ_STACK_SHARED, CBQ_FORM_PERSISTENT};
+    cbq_launch_config cfg{CBQ_KERNEL_AUTO, 0, 0, 0, CBQ_STACK_SHARED, CBQ_FORM_PERSISTENT, 1, 0};
 
     // Staging for cbq_intersect_host.
     std::mutex staging_lock;
