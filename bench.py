@@ -173,6 +173,15 @@ def profiled_traffic(workload: str):
     return float(m.group(1)) if m else None
 
 
+def profiled_issue_active(workload: str):
+    """smsp__issue_active (% of issue slots) of the traversal from the committed ncu summary."""
+    f = ROOT / "profiles" / f"traverse_{workload}.md"
+    if not f.exists():
+        return None
+    m = re.search(r"\| smsp__issue_active \| ([0-9.]+)%", f.read_text())
+    return float(m.group(1)) if m else None
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -361,6 +370,8 @@ def run_gpu(args, world, rank, local):
         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
         "peak_source": f"{peak_kind} hbm_gbs", "kernel": kernel_name,
         "traffic": None if traffic_per_ray is None else traffic_per_ray * rays_per_step / len(dev_batches),
+        "limiter": {"kind": "instruction issue (dependent node fetches are served from L2)",
+                    "issue_active_pct": profiled_issue_active(args.workload), "source": "ncu --set full"},
         "bytes_per_ray": {b[0]: RAY_BYTES + b[4] * SECTOR + HIT_BYTES for b in dev_batches},
         "fetches_per_ray": {b[0]: b[4] for b in dev_batches},
         "l2": {"achieved_gbs": achieved, "stream_peak_gbs": l2_stream, "frac_stream": achieved / l2_stream,

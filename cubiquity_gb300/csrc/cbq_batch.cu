@@ -33,15 +33,14 @@ struct BatchSrc {
 
 constexpr unsigned kFullMask = 0xffffffffu;
 
+// Descent stack in local memory and `steps` ESVO steps per loop iteration:
+// the faster choices for the single-volume kernel on GB300.
 __global__ void __launch_bounds__(256) cbq_k_flat_batch(const JobDesc* __restrict__ jobs, uint32_t njobs,
                                                         uint64_t total, unsigned long long* __restrict__ counter,
-                                                        uint32_t refill_min, uint32_t stack_rows)
+                                                        uint32_t refill_min, uint32_t steps)
 {
-    extern __shared__ uint32_t smem[];
-    SharedStack stack;
-    stack.base = smem + threadIdx.x;
-    stack.stride = blockDim.x;
-    uint64_t* prefix = reinterpret_cast<uint64_t*>(smem + (size_t)stack_rows * blockDim.x);
+    extern __shared__ uint64_t prefix[];  // njobs + 1 entries
+    LocalStack stack;
     for (uint32_t j = threadIdx.x; j <= njobs; j += blockDim.x) prefix[j] = j < njobs ? jobs[j].first : total;
     __syncthreads();
 
@@ -86,7 +85,7 @@ __global__ void __launch_bounds__(256) cbq_k_flat_batch(const JobDesc* __restric
             continue;
         }
         lane_settle(L, c);
-        if (L.mode == kLaneWalk) lane_walk(L, c, stack);
+        for (uint32_t k = 0; k < steps && L.mode == kLaneWalk; k++) lane_walk(L, c, stack);
     }
 }
 
@@ -107,11 +106,12 @@ void fill_job_volume(dev::JobDesc& d, const cbq_dag* dag)
 }
 
 cbq_status launch_batch_kernel(const dev::JobDesc* d_jobs, uint32_t njobs, uint64_t total, uint64_t* counter,
-                               int block, uint32_t refill, uint32_t stack_rows, int device, cudaStream_t s)
+                               int block, uint32_t refill, uint32_t steps, int device, cudaStream_t s)
 {
     if (total == 0 || njobs == 0) return CBQ_OK;
+    if (steps == 0) steps = 1;
     if (cudaMemsetAsync(counter, 0, sizeof(uint64_t), s) != cudaSuccess) return CBQ_ERR_CUDA;
-    const size_t smem = (size_t)stack_rows * block * 4 + (size_t)(njobs + 1) * 8;
+    const size_t smem = (size_t)(njobs + 1) * 8;  // the prefix offsets
     if (smem > 227u * 1024u) return CBQ_ERR_CAPACITY;
     if (smem > 48u * 1024u &&
         cudaFuncSetAttribute(dev::cbq_k_flat_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
@@ -123,7 +123,7 @@ cbq_status launch_batch_kernel(const dev::JobDesc* d_jobs, uint32_t njobs, uint6
         return CBQ_ERR_CUDA;
     per_sm = std::max(per_sm, 1);
     dev::cbq_k_flat_batch<<<sms * per_sm, block, smem, s>>>(d_jobs, njobs, total, (unsigned long long*)counter,
-                                                            refill, stack_rows);
+                                                            refill, steps);
     return cudaGetLastError() == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
 }
 
@@ -143,7 +143,7 @@ struct cbq_batch {
     dev::JobDesc* d_jobs = nullptr;
     uint32_t njobs = 0;                     // jobs in the device table
     uint64_t total = 0;
-    uint32_t stack_rows = 1;
+    uint32_t steps = kBatchStepsDefault;
     uint64_t* d_counter = nullptr;
     cbq_query query{1, CBQ_MAX_FOOTPRINT_DISABLED, 0u, 0u};
     int block = kBatchBlockDefault;
@@ -160,8 +160,8 @@ cbq_status enqueue_batch(cbq_batch* b, cudaStream_t s)
         cbq_status st = cbq_intersect(jb.dag, &jb.rays, jb.ray_count, &b->query, &jb.hits, (cbq_stream_t)s);
         if (st != CBQ_OK) return st;
     }
-    return launch_batch_kernel(b->d_jobs, b->njobs, b->total, b->d_counter, b->block, b->refill, b->stack_rows,
-                               b->device, s);
+    return launch_batch_kernel(b->d_jobs, b->njobs, b->total, b->d_counter, b->block, b->refill, b->steps, b->device,
+                               s);
 }
 
 void drop_graph(cbq_batch* b)
@@ -208,7 +208,6 @@ cbq_status cbq_batch_create(const cbq_job* jobs, int32_t job_count, const cbq_qu
     b->device = device;
     if (query) b->query = *query;
     uint64_t first = 0;
-    int32_t rows = 1;
     for (int32_t j = 0; j < job_count; j++) {
         const cbq_job& jb = jobs[j];
         if (!jb.dag || jb.dag->device != device) { delete b; return CBQ_ERR_INVALID_ARGUMENT; }
@@ -240,11 +239,9 @@ cbq_status cbq_batch_create(const cbq_job* jobs, int32_t job_count, const cbq_qu
         d.q.flags = b->query.flags;
         table.push_back(d);
         first += jb.ray_count;
-        rows = std::max(rows, jb.dag->max_height);
     }
     b->njobs = (uint32_t)table.size();
     b->total = first;
-    b->stack_rows = (uint32_t)rows;
     if (cudaMalloc((void**)&b->d_counter, 256 + table.size() * sizeof(dev::JobDesc)) != cudaSuccess) {
         cudaGetLastError();
         delete b;

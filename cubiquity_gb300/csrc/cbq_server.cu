@@ -145,7 +145,6 @@ cbq_status cbq_server::enqueue(Slot& s, const std::vector<Request*>& group)
 {
     uint32_t njobs = 0;
     uint64_t total = 0;
-    uint32_t rows = 1;
     for (Request* rq : group) {
         const uint64_t n = rq->r.ray_count;
         char* p = d_pool + rq->offset;
@@ -183,14 +182,13 @@ cbq_status cbq_server::enqueue(Slot& s, const std::vector<Request*>& group)
         jd.first = total;
         s.h_table[njobs++] = jd;
         total += n;
-        rows = std::max<uint32_t>(rows, (uint32_t)rq->r.dag->max_height);
     }
     if (njobs) {
         if (cudaMemcpyAsync(s.d_table, s.h_table, njobs * sizeof(dev::JobDesc), cudaMemcpyHostToDevice, s.stream) !=
             cudaSuccess)
             return CBQ_ERR_CUDA;
-        cbq_status st = launch_batch_kernel(s.d_table, njobs, total, s.d_counter, cfg.block, cfg.refill_min, rows,
-                                            device, s.stream);
+        cbq_status st = launch_batch_kernel(s.d_table, njobs, total, s.d_counter, cfg.block, cfg.refill_min,
+                                            kBatchStepsDefault, device, s.stream);
         if (st != CBQ_OK) return st;
     }
     // Results back to the host.

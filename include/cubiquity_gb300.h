@@ -172,7 +172,7 @@ cbq_status cbq_intersect_auto(const cbq_dag* dag, const cbq_rays* rays, uint64_t
                               const cbq_hits* hits, void* scratch, uint64_t scratch_bytes, cbq_stream_t stream);
 
 /* Autotuner: times every form x block {64,128,256} x refill {4,8,16} x stack
- * {shared, local} x steps {1,2} on these rays (synchronous; `repetitions`
+ * {shared, local} x steps {2,4,8} on these rays (synchronous; `repetitions`
  * launches each),
  * stores the fastest in the DAG's launch config and returns it with its time. */
 cbq_status cbq_autotune(cbq_dag* dag, const cbq_rays* rays, uint64_t n, const cbq_query* query,

@@ -35,14 +35,14 @@ def _same(a, b):
 
 @pytest.mark.parametrize("form", [cbq.FORM_PLAIN, cbq.FORM_PERSISTENT, cbq.FORM_SORTED])
 @pytest.mark.parametrize("stack", [cbq.STACK_SHARED, cbq.STACK_LOCAL])
-@pytest.mark.parametrize("block", [64, 256])
-def test_every_form_equals_the_drop_in(scene, form, stack, block):
+@pytest.mark.parametrize("block,steps", [(64, 1), (256, 3), (128, 8)])
+def test_every_form_equals_the_drop_in(scene, form, stack, block, steps):
     dag, rays = scene
     scratch = cbq.scratch_for(max(o.shape[0] for o, _ in rays.values()))
     for label, (o, d) in rays.items():
-        dag.set_launch_config(cbq.KERNEL_FLAT, 64, 0, 0, cbq.STACK_SHARED, cbq.FORM_PLAIN)
-        want = cbq.intersect_volume(dag, o, d)
-        dag.set_launch_config(cbq.KERNEL_FLAT, block, 0, 4, stack, form)
+        dag.set_launch_config(cbq.KERNEL_NESTED)
+        want = cbq.intersect_volume(dag, o, d)  # the reference's loop structure as written
+        dag.set_launch_config(cbq.KERNEL_FLAT, block, 0, 4, stack, form, steps)
         got = cbq.intersect_auto(dag, o, d, scratch)
         _same(got, want)
     dag.set_launch_config()
