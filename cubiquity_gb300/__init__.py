@@ -172,6 +172,19 @@ def sphere_rays(lo, hi, n: int, seed: int) -> tuple[np.ndarray, np.ndarray]:
     return o, d
 
 
+LOG_DEBUG, LOG_INFO, LOG_WARNING = 0, 1, 2
+LOG_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int32, ctypes.c_char_p)
+_sig("cbq_set_log_handler", [LOG_FN, ctypes.c_void_p], None)
+_log_keep = [None]
+
+
+def set_log_handler(fn) -> None:
+    """Routes the library's diagnostics to fn(level, message); None disables."""
+    cb = LOG_FN(lambda user, level, msg: fn(level, msg.decode(errors="replace"))) if fn else LOG_FN()
+    _log_keep[0] = cb
+    _lib.cbq_set_log_handler(cb, None)
+
+
 def _check(status: int, what: str) -> None:
     if status != 0:
         raise CbqError(status, what)
@@ -542,6 +555,7 @@ _sig("cbq_server_create", [ctypes.POINTER(_ServerConfig), ctypes.POINTER(_P)])
 _sig("cbq_server_submit", [_P, ctypes.POINTER(_Request), ctypes.POINTER(_U64)])
 _sig("cbq_server_wait", [_P, _U64, ctypes.c_int64])
 _sig("cbq_server_poll", [_P, _U64, ctypes.POINTER(ctypes.c_int32)])
+_sig("cbq_server_cancel", [_P, _U64])
 _sig("cbq_server_get_stats", [_P, ctypes.POINTER(_ServerStats)])
 _sig("cbq_server_reset_stats", [_P])
 _sig("cbq_server_destroy", [_P])
@@ -584,6 +598,10 @@ class Server:
             self._keep.pop(ticket, None)
         _check(st, "cbq_server_wait")
         return st
+
+    def cancel(self, ticket: int) -> int:
+        """Withdraws a request not yet launched; returns the status (0, 7 busy, 8 unknown)."""
+        return _lib.cbq_server_cancel(self._h, ticket)
 
     def poll(self, ticket: int) -> bool:
         done = ctypes.c_int32()

@@ -161,6 +161,9 @@ cbq_status cbq_dag_create(const uint32_t* host_nodes, uint64_t node_count, uint3
     if (e != cudaSuccess) { cudaGetLastError(); delete dag; return CBQ_ERR_OUT_OF_MEMORY; }
     e = cudaMemcpy(dag->d_nodes, host_nodes, bytes, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) { cudaFree(dag->d_nodes); delete dag; return CBQ_ERR_CUDA; }
+    cbq::log(CBQ_LOG_INFO, "DAG uploaded to device %d: %llu nodes (%.1f MB), root %u, max sub-DAG height %d, %s kernel",
+             dag->device, (unsigned long long)node_count, bytes / 1e6, root, dag->max_height,
+             dag->flat_ok ? "flat" : "nested (coordinates beyond 2^24)");
     *out = dag;
     return CBQ_OK;
 }
@@ -327,6 +330,10 @@ cbq_status cbq_autotune(cbq_dag* dag, const cbq_rays* rays, uint64_t n, const cb
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     dag->cfg = st == CBQ_OK ? winner : saved;
+    if (st == CBQ_OK)
+        cbq::log(CBQ_LOG_INFO, "autotune over %llu rays: form %d, block %d, refill %u, stack %s, steps %d: %.3f ms",
+                 (unsigned long long)n, winner.form, winner.block, winner.refill_min,
+                 winner.stack == CBQ_STACK_LOCAL ? "local" : "shared", winner.steps, win_ms);
     if (best) *best = dag->cfg;
     if (best_ms) *best_ms = st == CBQ_OK ? win_ms : 0.0f;
     return st;

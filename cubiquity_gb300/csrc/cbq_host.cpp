@@ -4,7 +4,10 @@
 #include "cbq_builder.hpp"
 #include "cbq_internal.hpp"
 
+#include <atomic>
+#include <chrono>
 #include <cmath>
+#include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -62,6 +65,23 @@ cbq_status validate_nodes(const uint32_t* nodes, uint64_t node_count, uint32_t r
     return CBQ_OK;
 }
 
+namespace {
+std::atomic<cbq_log_fn> g_log_fn{nullptr};
+std::atomic<void*> g_log_user{nullptr};
+}  // namespace
+
+void log(int level, const char* fmt, ...)
+{
+    cbq_log_fn fn = g_log_fn.load();
+    if (!fn) return;
+    char buf[512];
+    va_list args;
+    va_start(args, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, args);
+    va_end(args);
+    fn(g_log_user.load(), level, buf);
+}
+
 cbq_status validate_heights(const uint32_t* nodes, uint64_t node_count, const cbq_subdag subdags[8])
 {
     // Heights (0..31) at which each internal node has been reached.
@@ -109,6 +129,12 @@ const char* cbq_status_string(cbq_status s)
 }
 
 int cbq_abi_version(void) { return CBQ_ABI_VERSION; }
+
+void cbq_set_log_handler(cbq_log_fn fn, void* user)
+{
+    g_log_user.store(user);
+    g_log_fn.store(fn);
+}
 
 cbq_status cbq_dag_validate(const uint32_t* nodes, uint64_t node_count, uint32_t root)
 {
@@ -240,7 +266,11 @@ cbq_status cbq_build_scene(cbq_scene_kind kind, int edge_log2, uint64_t seed, in
     try {
         std::unique_ptr<Scene> scene = make_scene(kind, edge_log2, seed, param);
         if (!scene) return CBQ_ERR_INVALID_ARGUMENT;
+        const auto t0 = std::chrono::steady_clock::now();
         NodeArray arr = build_dag(*scene, threads);
+        cbq::log(CBQ_LOG_INFO, "built scene kind %d edge 2^%d seed %llu: %llu nodes in %.3f s", (int)kind, edge_log2,
+                 (unsigned long long)seed, (unsigned long long)arr.node_count(),
+                 std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
         uint32_t* out = (uint32_t*)std::malloc(arr.words.size() * 4);
         if (!out) return CBQ_ERR_OUT_OF_MEMORY;
         std::memcpy(out, arr.words.data(), arr.words.size() * 4);

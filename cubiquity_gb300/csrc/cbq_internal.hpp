@@ -16,6 +16,13 @@ cbq_status find_subdags(const uint32_t* nodes, uint64_t node_count, uint32_t roo
 // Full structural check of a host node array.
 cbq_status validate_nodes(const uint32_t* nodes, uint64_t node_count, uint32_t root);
 
+// printf-style message to the registered log handler (no-op without one).
+void log(int level, const char* fmt, ...)
+#if defined(__GNUC__)
+    __attribute__((format(printf, 2, 3)))
+#endif
+    ;
+
 // Checks that no internal node is reachable from a SubDAG root at height 0
 // (which also excludes cycles), so a traversal never descends below the leaves.
 cbq_status validate_heights(const uint32_t* nodes, uint64_t node_count, const cbq_subdag subdags[8]);

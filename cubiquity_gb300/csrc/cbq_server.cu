@@ -386,6 +386,24 @@ cbq_status cbq_server_wait(cbq_server* s, uint64_t ticket, int64_t timeout_us)
     return st;
 }
 
+cbq_status cbq_server_cancel(cbq_server* s, uint64_t ticket)
+{
+    if (!s) return CBQ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (auto it = s->queue.begin(); it != s->queue.end(); ++it) {
+        if ((*it)->ticket != ticket) continue;
+        Request* rq = *it;
+        s->queue.erase(it);
+        s->live.erase(ticket);
+        s->finished[ticket] = CBQ_ERR_CANCELLED;
+        delete rq;
+        s->cv_done.notify_all();
+        return CBQ_OK;
+    }
+    if (s->live.count(ticket)) return CBQ_ERR_BUSY;  // already launched: it will complete
+    return CBQ_ERR_NOT_FOUND;
+}
+
 cbq_status cbq_server_poll(cbq_server* s, uint64_t ticket, int32_t* done)
 {
     if (!s || !done) return CBQ_ERR_INVALID_ARGUMENT;

@@ -107,6 +107,16 @@ typedef struct cbq_dag_info {
 const char* cbq_status_string(cbq_status s);
 int cbq_abi_version(void);
 
+/* Diagnostics callback, in the spirit of the reference's set_debug_handler /
+ * set_warning_handler (base.h:102-107): the library reports DAG uploads, scene
+ * builds, autotuner choices and server events.  NULL disables.  The callback
+ * may run on library threads (the server's). */
+#define CBQ_LOG_DEBUG 0
+#define CBQ_LOG_INFO 1
+#define CBQ_LOG_WARNING 2
+typedef void (*cbq_log_fn)(void* user, int32_t level, const char* message);
+void cbq_set_log_handler(cbq_log_fn fn, void* user);
+
 /* Checks that every child index (and the root) is < node_count and that slots
  * 0..255 are material nodes.  Host memory. */
 cbq_status cbq_dag_validate(const uint32_t* nodes, uint64_t node_count, uint32_t root);
@@ -309,6 +319,10 @@ cbq_status cbq_server_submit(cbq_server* s, const cbq_request* r, uint64_t* tick
  * unknown or already-waited ticket. */
 cbq_status cbq_server_wait(cbq_server* s, uint64_t ticket, int64_t timeout_us);
 cbq_status cbq_server_poll(cbq_server* s, uint64_t ticket, int32_t* done);
+/* Withdraws a request that has not been launched yet: its wait then returns
+ * CBQ_ERR_CANCELLED and its buffers are never touched again.  CBQ_ERR_BUSY if it
+ * is already on the device (it will complete), CBQ_ERR_NOT_FOUND if unknown. */
+cbq_status cbq_server_cancel(cbq_server* s, uint64_t ticket);
 cbq_status cbq_server_get_stats(cbq_server* s, cbq_server_stats* out);
 cbq_status cbq_server_reset_stats(cbq_server* s);
 /* Finishes every queued and running request, then stops. */

@@ -150,6 +150,19 @@ def test_relocated_scene_voxels_and_subdags():
     assert len(sd) == 1 and tuple(sd[0].lower_bound) == origin
 
 
+def test_log_handler_receives_library_messages():
+    got = []
+    cbq.set_log_handler(lambda level, msg: got.append((level, msg)))
+    try:
+        W.SceneSpec(cbq.SCENE_SPHERES, 5, 3, 6).build()
+    finally:
+        cbq.set_log_handler(None)
+    assert any(level == cbq.LOG_INFO and "built scene" in msg for level, msg in got)
+    n = len(got)
+    W.SceneSpec(cbq.SCENE_SPHERES, 5, 3, 6).build()
+    assert len(got) == n  # disabled
+
+
 def test_bounce_rays_are_unit_and_in_hemisphere():
     pos = np.array([[1.0, 2.0, 3.0], [5.0, 5.0, 5.0]], np.float32)
     nrm = np.array([[0.0, 0.0, 1.0], [-1.0, 0.0, 0.0]], np.float32)

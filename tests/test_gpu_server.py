@@ -108,6 +108,26 @@ def test_submissions_from_several_threads(served):
     server.close()
 
 
+def test_cancel_queued_request(served):
+    dags, pools = served
+    (co, cd), _ = pools[0]
+    # One launch slot and room for one request at a time: later requests queue.
+    server = cbq.Server(device_memory_budget=1 << 20, max_inflight_launches=1)
+    tickets = [server.submit(dags[0], co[:9000], cd[:9000])[0] for _ in range(6)]
+    st = server.cancel(tickets[-1])
+    assert st in (0, 7)  # cancelled while queued, or (if the GPU raced ahead) already launched
+    for t in tickets[:-1]:
+        assert server.wait(t) == 0
+    if st == 0:
+        with pytest.raises(cbq.CbqError) as e:
+            server.wait(tickets[-1])
+        assert e.value.status == 9  # CBQ_ERR_CANCELLED
+    else:
+        assert server.wait(tickets[-1]) == 0
+    assert server.cancel(tickets[0]) == 8  # finished and collected: unknown
+    server.close()
+
+
 def test_admission_capacity_timeout_and_shutdown(served):
     dags, pools = served
     (co, cd), _ = pools[0]
