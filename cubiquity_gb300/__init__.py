@@ -537,10 +537,13 @@ class _Request(ctypes.Structure):
                 ("ray_count", ctypes.c_uint64), ("query", _Query), ("host_hits", _Hits)]
 
 
+SERVER_ALWAYS_STAGE = 0x1
+
+
 class _ServerConfig(ctypes.Structure):
     _fields_ = [("device_memory_budget", ctypes.c_uint64), ("max_inflight_launches", ctypes.c_int32),
                 ("max_batch_requests", ctypes.c_int32), ("max_batch_rays", ctypes.c_uint64),
-                ("block", ctypes.c_int32), ("refill_min", ctypes.c_uint32)]
+                ("block", ctypes.c_int32), ("refill_min", ctypes.c_uint32), ("flags", ctypes.c_uint32)]
 
 
 class _ServerStats(ctypes.Structure):
@@ -548,7 +551,8 @@ class _ServerStats(ctypes.Structure):
                 ("launches", ctypes.c_uint64), ("queued", ctypes.c_uint64), ("inflight_launches", ctypes.c_uint64),
                 ("mean_requests_per_launch", ctypes.c_double), ("latency_p50_us", ctypes.c_double),
                 ("latency_p99_us", ctypes.c_double), ("latency_max_us", ctypes.c_double),
-                ("latency_mean_us", ctypes.c_double), ("busy_seconds", ctypes.c_double)]
+                ("latency_mean_us", ctypes.c_double), ("busy_seconds", ctypes.c_double),
+                ("direct_requests", ctypes.c_uint64)]
 
 
 _sig("cbq_server_create", [ctypes.POINTER(_ServerConfig), ctypes.POINTER(_P)])
@@ -565,12 +569,15 @@ class Server:
     """Continuous-batching request server over resident DAGs (cbq_server).
 
     submit() takes host numpy arrays and returns a ticket at once; the arrays
-    are kept alive here until the ticket is waited for."""
+    are kept alive here until the ticket is waited for.  Requests whose arrays
+    are all page-locked (e.g. from torch's pin_memory()) are served without
+    copies unless always_stage is set."""
 
     def __init__(self, device_memory_budget: int = 1 << 30, max_inflight_launches: int = 4,
-                 max_batch_requests: int = 256, max_batch_rays: int = 4 << 20, block: int = 0, refill_min: int = 0):
+                 max_batch_requests: int = 256, max_batch_rays: int = 4 << 20, block: int = 0, refill_min: int = 0,
+                 always_stage: bool = False):
         cfg = _ServerConfig(device_memory_budget, max_inflight_launches, max_batch_requests, max_batch_rays, block,
-                            refill_min)
+                            refill_min, SERVER_ALWAYS_STAGE if always_stage else 0)
         h = _P()
         _check(_lib.cbq_server_create(ctypes.byref(cfg), ctypes.byref(h)), "cbq_server_create")
         self._h = h

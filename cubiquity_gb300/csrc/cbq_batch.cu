@@ -23,8 +23,9 @@ struct BatchSrc {
     __device__ __forceinline__ const QueryParams& query(const Lane& L) const { return jobs[L.job].q; }
     __device__ __forceinline__ const uint32_t* nodes(const Lane& L) const { return L.nodes; }
     __device__ __forceinline__ const SubDag& subdag(const Lane& L, uint32_t k) const { return jobs[L.job].sd[k]; }
-    __device__ __forceinline__ float4 ray_origin(const Lane& L, uint64_t i) const { return __ldg(jobs[L.job].orig + i); }
-    __device__ __forceinline__ float4 ray_direction(const Lane& L, uint64_t i) const { return __ldg(jobs[L.job].dir + i); }
+    // Rays are read once (from device or page-locked host memory): streaming loads.
+    __device__ __forceinline__ float4 ray_origin(const Lane& L, uint64_t i) const { return __ldcs(jobs[L.job].orig + i); }
+    __device__ __forceinline__ float4 ray_direction(const Lane& L, uint64_t i) const { return __ldcs(jobs[L.job].dir + i); }
     __device__ __forceinline__ void write(const Lane& L, const RayResult& r) const
     {
         write_result(jobs[L.job].out, L.ray, r);

@@ -57,8 +57,9 @@ struct FlatCtx {
     __device__ __forceinline__ const QueryParams& query(const Lane&) const { return q; }
     __device__ __forceinline__ const uint32_t* nodes(const Lane&) const { return dag.nodes; }
     __device__ __forceinline__ const SubDag& subdag(const Lane&, uint32_t k) const { return dag.sd[k]; }
-    __device__ __forceinline__ float4 ray_origin(const Lane&, uint64_t i) const { return __ldg(orig + i); }
-    __device__ __forceinline__ float4 ray_direction(const Lane&, uint64_t i) const { return __ldg(dir + i); }
+    // Rays are read once: streaming loads (evict-first) leave L2 to the node store.
+    __device__ __forceinline__ float4 ray_origin(const Lane&, uint64_t i) const { return __ldcs(orig + i); }
+    __device__ __forceinline__ float4 ray_direction(const Lane&, uint64_t i) const { return __ldcs(dir + i); }
     __device__ __forceinline__ void write(const Lane& L, const RayResult& r) const
     {
         write_result(out, L.ray, r);

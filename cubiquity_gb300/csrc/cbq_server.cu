@@ -44,11 +44,52 @@ uint64_t request_bytes(uint64_t n) { return align_up(n * kBytesPerRay + 8 * kAli
 struct Request {
     uint64_t ticket = 0;
     cbq_request r{};
-    uint64_t bytes = 0;
+    uint64_t bytes = 0;      // pool bytes (0 for a direct request)
     uint64_t offset = 0;
+    bool direct = false;     // the kernel reads and writes the caller's (pinned) host buffers itself
+    const float* d_o = nullptr;
+    const float* d_d = nullptr;
+    cbq_hits d_hits{};
     Clock::time_point submitted;
     cbq_status status = CBQ_OK;
 };
+
+// The device address of host memory the GPU can use directly (page-locked and
+// mapped, or managed), or nullptr when the buffer has to be staged.
+const void* device_alias(const void* p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost && a.devicePointer) return a.devicePointer;
+    if (a.type == cudaMemoryTypeManaged) return p;
+    return nullptr;
+}
+
+// Resolves every buffer of a request to a device alias; false if any needs staging.
+bool resolve_direct(Request& rq)
+{
+    const cbq_request& r = rq.r;
+    if (((uintptr_t)r.host_origin_tmax & 15u) || ((uintptr_t)r.host_direction & 15u)) return false;
+    rq.d_o = (const float*)device_alias(r.host_origin_tmax);
+    rq.d_d = (const float*)device_alias(r.host_direction);
+    if (!rq.d_o || !rq.d_d) return false;
+    const cbq_hits& h = r.host_hits;
+    cbq_hits& d = rq.d_hits;
+    struct F { void* host; void** dev; };
+    const F fields[] = {{h.hit, (void**)&d.hit}, {h.distance, (void**)&d.distance}, {h.material, (void**)&d.material},
+                        {h.position, (void**)&d.position}, {h.normal, (void**)&d.normal},
+                        {h.voxel, (void**)&d.voxel}, {h.status, (void**)&d.status}};
+    for (const F& f : fields) {
+        *f.dev = nullptr;
+        if (!f.host) continue;
+        *f.dev = (void*)device_alias(f.host);
+        if (!*f.dev) return false;
+    }
+    return true;
+}
 
 // First-fit allocator over [0, size).
 class Pool {
@@ -133,6 +174,7 @@ struct cbq_server {
     // statistics
     std::vector<double> latencies_us;
     uint64_t submitted = 0, completed = 0, rays_completed = 0, launches = 0, launched_requests = 0;
+    uint64_t direct_completed = 0;
     Clock::time_point first_submit, last_complete;
     bool have_first = false;
 
@@ -147,6 +189,35 @@ cbq_status cbq_server::enqueue(Slot& s, const std::vector<Request*>& group)
     uint64_t total = 0;
     for (Request* rq : group) {
         const uint64_t n = rq->r.ray_count;
+        if (rq->direct) {  // the kernel reads the rays and writes the hits in host memory itself
+            dev::JobDesc jd;
+            std::memset(&jd, 0, sizeof(jd));
+            fill_job_volume(jd, rq->r.dag);
+            jd.orig = (const float4*)rq->d_o;
+            jd.dir = (const float4*)rq->d_d;
+            const cbq_hits& dh = rq->d_hits;
+            jd.out.hit = dh.hit;
+            jd.out.distance = dh.distance;
+            jd.out.material = dh.material;
+            jd.out.position = dh.position;
+            jd.out.normal = dh.normal;
+            jd.out.voxel = dh.voxel;
+            jd.out.status = dh.status;
+            jd.count = n;
+            jd.q.compute_surface = rq->r.query.compute_surface;
+            jd.q.max_footprint = rq->r.query.max_footprint;
+            jd.q.flags = rq->r.query.flags;
+            if (!rq->r.dag->flat_ok) {
+                cbq_rays rays{rq->d_o, rq->d_d};
+                cbq_status st = cbq_intersect(rq->r.dag, &rays, n, &rq->r.query, &dh, (cbq_stream_t)s.stream);
+                if (st != CBQ_OK) return st;
+                continue;
+            }
+            jd.first = total;
+            s.h_table[njobs++] = jd;
+            total += n;
+            continue;
+        }
         char* p = d_pool + rq->offset;
         float* o = (float*)p;
         float* d = (float*)(p + n * 16);
@@ -193,6 +264,7 @@ cbq_status cbq_server::enqueue(Slot& s, const std::vector<Request*>& group)
     }
     // Results back to the host.
     for (Request* rq : group) {
+        if (rq->direct) continue;
         const uint64_t n = rq->r.ray_count;
         char* h = d_pool + rq->offset + n * 32;
         const cbq_hits& hh = rq->r.host_hits;
@@ -221,7 +293,7 @@ void cbq_server::run_scheduler()
             Request* rq = queue.front();
             if (!group.empty() && rays + rq->r.ray_count > cfg.max_batch_rays) break;
             uint64_t off = 0;
-            if (!pool.alloc(rq->bytes, &off)) break;  // FIFO: wait for memory rather than skip ahead
+            if (rq->bytes && !pool.alloc(rq->bytes, &off)) break;  // FIFO: wait for memory rather than skip ahead
             rq->offset = off;
             group.push_back(rq);
             rays += rq->r.ray_count;
@@ -268,7 +340,8 @@ void cbq_server::run_completer()
         for (Request* rq : slots[si].reqs) {
             if (!ok && rq->status == CBQ_OK) rq->status = CBQ_ERR_CUDA;
             latencies_us.push_back(std::chrono::duration<double, std::micro>(now - rq->submitted).count());
-            pool.release(rq->offset, rq->bytes);
+            if (rq->bytes) pool.release(rq->offset, rq->bytes);
+            if (rq->direct) direct_completed++;
             finished[rq->ticket] = rq->status;
             live.erase(rq->ticket);
             completed++;
@@ -301,7 +374,7 @@ cbq_status cbq_server_create(const cbq_server_config* cfg, cbq_server** out)
     if (c.block <= 0) c.block = 128;
     if (c.refill_min == 0) c.refill_min = 8;
     if (c.block > 256 || (c.block % 32) || c.refill_min > 32 || c.max_inflight_launches > 64 ||
-        c.max_batch_requests > 65536) {
+        c.max_batch_requests > 65536 || (c.flags & ~(uint32_t)CBQ_SERVER_ALWAYS_STAGE)) {
         delete s;
         return CBQ_ERR_INVALID_ARGUMENT;
     }
@@ -343,13 +416,16 @@ cbq_status cbq_server_submit(cbq_server* s, const cbq_request* r, uint64_t* tick
     if (!s || !r || !ticket || !r->dag) return CBQ_ERR_INVALID_ARGUMENT;
     if (r->dag->device != s->device) return CBQ_ERR_INVALID_ARGUMENT;
     if (r->ray_count > 0 && (!r->host_origin_tmax || !r->host_direction)) return CBQ_ERR_INVALID_ARGUMENT;
-    const uint64_t bytes = request_bytes(r->ray_count);
-    if (bytes > s->cfg.device_memory_budget) return CBQ_ERR_CAPACITY;
     Request* rq = new (std::nothrow) Request();
     if (!rq) return CBQ_ERR_OUT_OF_MEMORY;
-    rq->r = *r;
-    rq->bytes = bytes;
     rq->submitted = Clock::now();
+    rq->r = *r;
+    rq->direct = r->ray_count > 0 && !(s->cfg.flags & CBQ_SERVER_ALWAYS_STAGE) && resolve_direct(*rq);
+    rq->bytes = rq->direct ? 0 : request_bytes(r->ray_count);
+    if (rq->bytes > s->cfg.device_memory_budget) {
+        delete rq;
+        return CBQ_ERR_CAPACITY;
+    }
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->stopping) { delete rq; return CBQ_ERR_SHUTDOWN; }
     rq->ticket = s->next_ticket++;
@@ -429,6 +505,7 @@ cbq_status cbq_server_get_stats(cbq_server* s, cbq_server_stats* out)
     double sum = 0;
     for (double v : s->latencies_us) sum += v;
     out->latency_mean_us = s->latencies_us.empty() ? 0.0 : sum / (double)s->latencies_us.size();
+    out->direct_requests = s->direct_completed;
     out->queued = s->queue.size();
     out->inflight_launches = s->inflight.size();
     if (s->have_first && s->completed)
@@ -442,6 +519,7 @@ cbq_status cbq_server_reset_stats(cbq_server* s)
     std::lock_guard<std::mutex> lk(s->mu);
     s->latencies_us.clear();
     s->submitted = s->completed = s->rays_completed = s->launches = s->launched_requests = 0;
+    s->direct_completed = 0;
     s->have_first = false;
     return CBQ_OK;
 }

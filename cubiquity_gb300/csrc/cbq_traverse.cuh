@@ -317,20 +317,22 @@ __device__ __forceinline__ RayResult intersect_volume(const DagParams& dag, floa
     return r;
 }
 
+// Hit records are written once and not read back by the kernel: streaming
+// (evict-first) stores keep them from displacing the node store in L2.
 __device__ __forceinline__ void write_result(const HitsOut& out, size_t i, const RayResult& r)
 {
-    if (out.hit) out.hit[i] = r.hit ? 1 : 0;
-    if (out.distance) out.distance[i] = r.distance;
-    if (out.material) out.material[i] = r.material;
+    if (out.hit) __stcs(out.hit + i, (uint8_t)(r.hit ? 1 : 0));
+    if (out.distance) __stcs(out.distance + i, r.distance);
+    if (out.material) __stcs(out.material + i, r.material);
     if (out.position) {
-        out.position[3 * i] = r.px;
-        out.position[3 * i + 1] = r.py;
-        out.position[3 * i + 2] = r.pz;
+        __stcs(out.position + 3 * i, r.px);
+        __stcs(out.position + 3 * i + 1, r.py);
+        __stcs(out.position + 3 * i + 2, r.pz);
     }
     if (out.normal) {
-        out.normal[3 * i] = r.nx;
-        out.normal[3 * i + 1] = r.ny;
-        out.normal[3 * i + 2] = r.nz;
+        __stcs(out.normal + 3 * i, r.nx);
+        __stcs(out.normal + 3 * i + 1, r.ny);
+        __stcs(out.normal + 3 * i + 2, r.nz);
     }
     if (out.voxel) {
         int32_t vx = 0, vy = 0, vz = 0;
@@ -339,11 +341,11 @@ __device__ __forceinline__ void write_result(const HitsOut& out, size_t i, const
             vy = __float2int_rd(__fadd_rn(__fsub_rn(r.py, __fmul_rn(0.5f, r.ny)), 0.5f));
             vz = __float2int_rd(__fadd_rn(__fsub_rn(r.pz, __fmul_rn(0.5f, r.nz)), 0.5f));
         }
-        out.voxel[3 * i] = vx;
-        out.voxel[3 * i + 1] = vy;
-        out.voxel[3 * i + 2] = vz;
+        __stcs(out.voxel + 3 * i, vx);
+        __stcs(out.voxel + 3 * i + 1, vy);
+        __stcs(out.voxel + 3 * i + 2, vz);
     }
-    if (out.status) out.status[i] = (uint8_t)r.status;
+    if (out.status) __stcs(out.status + i, (uint8_t)r.status);
 }
 
 }  // namespace dev

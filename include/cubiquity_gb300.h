@@ -293,7 +293,16 @@ typedef struct cbq_server_config {
     uint64_t max_batch_rays;        /* rays per launch (0 = 4 Mi) */
     int32_t block;                  /* threads per block (0 = 128) */
     uint32_t refill_min;            /* idle lanes that trigger a refill (0 = 8) */
+    uint32_t flags;                 /* CBQ_SERVER_* */
 } cbq_server_config;
+
+/* A request whose ray and hit buffers are all device-accessible host memory
+ * (page-locked by cudaHostAlloc / cudaHostRegister, or managed) and whose rays
+ * are 16-byte aligned is served directly: the kernel reads its rays and writes
+ * its hits in host memory, it takes no room in the memory budget and no copy is
+ * issued for it.  Other requests are staged through the budget with copies.
+ * This flag stages every request. */
+#define CBQ_SERVER_ALWAYS_STAGE 0x1u
 
 typedef struct cbq_server_stats {
     uint64_t submitted, completed, rays_completed, launches;
@@ -301,6 +310,7 @@ typedef struct cbq_server_stats {
     double mean_requests_per_launch;
     double latency_p50_us, latency_p99_us, latency_max_us, latency_mean_us; /* submit -> hits on host */
     double busy_seconds;            /* first submit -> last completion */
+    uint64_t direct_requests;       /* completed requests served from host memory without copies */
 } cbq_server_stats;
 
 /* Continuous batching: requests are admitted in arrival order while the memory

@@ -151,3 +151,35 @@ def test_admission_capacity_timeout_and_shutdown(served):
     want = cbq.intersect_volume_host(dags[1], co[:5000], cd[:5000])
     for out in pending:
         _same(out, want)
+
+
+def _pinned(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+
+
+def test_page_locked_requests_are_served_without_copies(served):
+    """Requests whose buffers are all page-locked host memory are traversed in
+    place (no copies, no budget); the hits equal the staged path's."""
+    dags, pools = served
+    (co, cd), (vo, vd) = pools[2]
+    cases = [(co[:7000], cd[:7000], True), (vo[100:5100], vd[100:5100], False), (co[9001:9002], cd[9001:9002], True)]
+    direct = cbq.Server(device_memory_budget=1 << 20)  # too small for any of these if they were staged
+    staged = cbq.Server(device_memory_budget=64 << 20, always_stage=True)
+    for o, d, coll in cases:
+        po, pd = _pinned(o), _pinned(d)
+        out = {k: _pinned(v) for k, v in cbq.alloc_host_hits(o.shape[0]).items()}
+        t, got = direct.submit(dags[2], po, pd, _query(coll), out=out)
+        assert direct.wait(t) == 0
+        t2, want = staged.submit(dags[2], po, pd, _query(coll))
+        assert staged.wait(t2) == 0
+        _same(got, want)
+        _same(got, cbq.intersect_volume_host(dags[2], o, d, use_tmax=coll))
+    assert direct.stats()["direct_requests"] == len(cases)
+    assert staged.stats()["direct_requests"] == 0
+    # Pageable outputs: the request is staged (and still correct).
+    t, got = direct.submit(dags[2], _pinned(co[:2000]), _pinned(cd[:2000]), _query(True))
+    assert direct.wait(t) == 0
+    _same(got, cbq.intersect_volume_host(dags[2], co[:2000], cd[:2000], use_tmax=True))
+    assert direct.stats()["direct_requests"] == len(cases)
+    direct.close()
+    staged.close()
