@@ -60,6 +60,9 @@ def parse_args():
     p.add_argument("--chunk", type=int, default=0, help="persistent: refill threshold (flat) / grab size (nested)")
     p.add_argument("--e2e-steps", type=int, default=5)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--serve-buffers", choices=["staged", "in-place"], default="staged",
+                   help="serve-8: stage requests through device memory with copies, or traverse the page-locked "
+                        "request buffers in place")
     args = p.parse_args()
     args.persistent = args.form == "persistent"
     return args
@@ -645,8 +648,9 @@ def run_gpu_serve(args, world, rank, local):
              "material": torch.empty(max_n, dtype=torch.int32).pin_memory().numpy(),
              "voxel": torch.empty((max_n, 3), dtype=torch.int32).pin_memory().numpy(),
              "status": torch.empty(max_n, dtype=torch.uint8).pin_memory().numpy()} for _ in range(ring)]
+    in_place = args.serve_buffers == "in-place"
     server = cbq.Server(device_memory_budget=2 << 30, max_inflight_launches=4, max_batch_requests=128,
-                        max_batch_rays=4 << 20)
+                        max_batch_rays=4 << 20, in_place=in_place)
     queries = {True: cbq.Query(True, cbq.MAX_FOOTPRINT_DISABLED, True), False: cbq.Query()}
 
     def submit(k, r):
@@ -670,15 +674,14 @@ def run_gpu_serve(args, world, rank, local):
         return time.perf_counter() - t0
 
     n_peak = 3000
-    # The same closed loop through a server that stages every request through
-    # device memory with copies (the path for pageable host buffers).
+    # The same closed loop through a server of the other buffer mode.
     live = server
     server = cbq.Server(device_memory_budget=2 << 30, max_inflight_launches=4, max_batch_requests=128,
-                        max_batch_rays=4 << 20, always_stage=True)
+                        max_batch_rays=4 << 20, in_place=not in_place)
     closed_loop(0, 300)
     server.reset_stats()
-    dt_staged = closed_loop(300, n_peak)
-    staged = server.stats()
+    dt_other = closed_loop(300, n_peak)
+    other = server.stats()
     server.close()
     server = live
 
@@ -740,12 +743,14 @@ def run_gpu_serve(args, world, rank, local):
         "data": "synthetic (8 seeded terrain DAGs, 1k-256k-ray requests: 70% collision tmax<=64, 30% view)",
         "config": {"workload": "serve-8", "edges": [1 << s.edge_log2 for s in scenes],
                    "server": {"memory_budget_gb": 2, "inflight_launches": 4, "max_batch_requests": 128,
-                              "buffers": "page-locked host (served in place)"},
+                              "buffers": "page-locked host, served in place" if in_place else
+                              "page-locked host, staged through device memory"},
                    "arrivals": "open-loop Poisson"},
         "peak": {"requests_per_s": peak_rps, "mrays_per_s": peak_mrays, "p50_ms": peak["latency_p50_us"] / 1e3,
                  "p99_ms": peak["latency_p99_us"] / 1e3, "direct_requests": peak["direct_requests"]},
-        "peak_staged": {"requests_per_s": n_peak / dt_staged, "mrays_per_s": staged["rays_completed"] / dt_staged / 1e6,
-                        "p50_ms": staged["latency_p50_us"] / 1e3, "p99_ms": staged["latency_p99_us"] / 1e3},
+        "peak_other_buffers": {"buffers": "staged" if in_place else "in-place", "requests_per_s": n_peak / dt_other,
+                               "mrays_per_s": other["rays_completed"] / dt_other / 1e6,
+                               "p50_ms": other["latency_p50_us"] / 1e3, "p99_ms": other["latency_p99_us"] / 1e3},
         "half_load": half, "sweep": sweep,
         "e2e": {"value": half["mrays_per_s"], "unit": "Mrays/s", "note": "host rays in, host hits out, per request"},
         "gpu_launches": None, "clocks": clk,

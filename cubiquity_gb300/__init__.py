@@ -537,7 +537,7 @@ class _Request(ctypes.Structure):
                 ("ray_count", ctypes.c_uint64), ("query", _Query), ("host_hits", _Hits)]
 
 
-SERVER_ALWAYS_STAGE = 0x1
+SERVER_IN_PLACE = 0x1
 
 
 class _ServerConfig(ctypes.Structure):
@@ -569,15 +569,15 @@ class Server:
     """Continuous-batching request server over resident DAGs (cbq_server).
 
     submit() takes host numpy arrays and returns a ticket at once; the arrays
-    are kept alive here until the ticket is waited for.  Requests whose arrays
-    are all page-locked (e.g. from torch's pin_memory()) are served without
-    copies unless always_stage is set."""
+    are kept alive here until the ticket is waited for.  With in_place=True,
+    requests whose arrays are all page-locked (e.g. from torch's pin_memory())
+    are traversed in host memory without copies or device memory."""
 
     def __init__(self, device_memory_budget: int = 1 << 30, max_inflight_launches: int = 4,
                  max_batch_requests: int = 256, max_batch_rays: int = 4 << 20, block: int = 0, refill_min: int = 0,
-                 always_stage: bool = False):
+                 in_place: bool = False):
         cfg = _ServerConfig(device_memory_budget, max_inflight_launches, max_batch_requests, max_batch_rays, block,
-                            refill_min, SERVER_ALWAYS_STAGE if always_stage else 0)
+                            refill_min, SERVER_IN_PLACE if in_place else 0)
         h = _P()
         _check(_lib.cbq_server_create(ctypes.byref(cfg), ctypes.byref(h)), "cbq_server_create")
         self._h = h

@@ -46,7 +46,7 @@ struct Request {
     cbq_request r{};
     uint64_t bytes = 0;      // pool bytes (0 for a direct request)
     uint64_t offset = 0;
-    bool direct = false;     // the kernel reads and writes the caller's (pinned) host buffers itself
+    bool direct = false;     // served in place: the kernel reads and writes the caller's host buffers
     const float* d_o = nullptr;
     const float* d_d = nullptr;
     cbq_hits d_hits{};
@@ -374,7 +374,7 @@ cbq_status cbq_server_create(const cbq_server_config* cfg, cbq_server** out)
     if (c.block <= 0) c.block = 128;
     if (c.refill_min == 0) c.refill_min = 8;
     if (c.block > 256 || (c.block % 32) || c.refill_min > 32 || c.max_inflight_launches > 64 ||
-        c.max_batch_requests > 65536 || (c.flags & ~(uint32_t)CBQ_SERVER_ALWAYS_STAGE)) {
+        c.max_batch_requests > 65536 || (c.flags & ~(uint32_t)CBQ_SERVER_IN_PLACE)) {
         delete s;
         return CBQ_ERR_INVALID_ARGUMENT;
     }
@@ -420,7 +420,7 @@ cbq_status cbq_server_submit(cbq_server* s, const cbq_request* r, uint64_t* tick
     if (!rq) return CBQ_ERR_OUT_OF_MEMORY;
     rq->submitted = Clock::now();
     rq->r = *r;
-    rq->direct = r->ray_count > 0 && !(s->cfg.flags & CBQ_SERVER_ALWAYS_STAGE) && resolve_direct(*rq);
+    rq->direct = r->ray_count > 0 && (s->cfg.flags & CBQ_SERVER_IN_PLACE) && resolve_direct(*rq);
     rq->bytes = rq->direct ? 0 : request_bytes(r->ray_count);
     if (rq->bytes > s->cfg.device_memory_budget) {
         delete rq;

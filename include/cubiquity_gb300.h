@@ -296,13 +296,16 @@ typedef struct cbq_server_config {
     uint32_t flags;                 /* CBQ_SERVER_* */
 } cbq_server_config;
 
-/* A request whose ray and hit buffers are all device-accessible host memory
- * (page-locked by cudaHostAlloc / cudaHostRegister, or managed) and whose rays
- * are 16-byte aligned is served directly: the kernel reads its rays and writes
- * its hits in host memory, it takes no room in the memory budget and no copy is
- * issued for it.  Other requests are staged through the budget with copies.
- * This flag stages every request. */
-#define CBQ_SERVER_ALWAYS_STAGE 0x1u
+/* By default every request is staged: rays copied into the device memory
+ * budget, hits copied back.  With CBQ_SERVER_IN_PLACE, a request whose ray and
+ * hit buffers are all device-accessible host memory (page-locked by
+ * cudaHostAlloc / cudaHostRegister, or managed) and whose rays are 16-byte
+ * aligned is served in place instead: the kernel reads its rays and writes its
+ * hits in host memory, it takes no room in the budget and no copy is issued.
+ * Hit stores across the host link are narrow, so in-place traversal runs at
+ * about half the staged rate; it suits small requests and clients that cannot
+ * spare device memory. */
+#define CBQ_SERVER_IN_PLACE 0x1u
 
 typedef struct cbq_server_stats {
     uint64_t submitted, completed, rays_completed, launches;
@@ -310,7 +313,7 @@ typedef struct cbq_server_stats {
     double mean_requests_per_launch;
     double latency_p50_us, latency_p99_us, latency_max_us, latency_mean_us; /* submit -> hits on host */
     double busy_seconds;            /* first submit -> last completion */
-    uint64_t direct_requests;       /* completed requests served from host memory without copies */
+    uint64_t direct_requests;       /* completed requests served in place (CBQ_SERVER_IN_PLACE) */
 } cbq_server_stats;
 
 /* Continuous batching: requests are admitted in arrival order while the memory

@@ -157,14 +157,15 @@ def _pinned(a):
     return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
 
 
-def test_page_locked_requests_are_served_without_copies(served):
-    """Requests whose buffers are all page-locked host memory are traversed in
-    place (no copies, no budget); the hits equal the staged path's."""
+def test_page_locked_requests_are_served_in_place(served):
+    """With in_place, requests whose buffers are all page-locked host memory are
+    traversed in host memory (no copies, no budget); the hits equal the staged
+    path's."""
     dags, pools = served
     (co, cd), (vo, vd) = pools[2]
     cases = [(co[:7000], cd[:7000], True), (vo[100:5100], vd[100:5100], False), (co[9001:9002], cd[9001:9002], True)]
-    direct = cbq.Server(device_memory_budget=1 << 20)  # too small for any of these if they were staged
-    staged = cbq.Server(device_memory_budget=64 << 20, always_stage=True)
+    direct = cbq.Server(device_memory_budget=1 << 20, in_place=True)  # too small for these if staged
+    staged = cbq.Server(device_memory_budget=64 << 20)
     for o, d, coll in cases:
         po, pd = _pinned(o), _pinned(d)
         out = {k: _pinned(v) for k, v in cbq.alloc_host_hits(o.shape[0]).items()}
