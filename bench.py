@@ -60,6 +60,8 @@ def parse_args():
     p.add_argument("--chunk", type=int, default=0, help="persistent: refill threshold (flat) / grab size (nested)")
     p.add_argument("--e2e-steps", type=int, default=5)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--layout", choices=["reference", "compact"], default="reference",
+                   help="device node store: the reference's array, or the compact store (occupied children only)")
     p.add_argument("--serve-buffers", choices=["staged", "in-place"], default="staged",
                    help="serve-8: stage requests through device memory with copies, or traverse the page-locked "
                         "request buffers in place")
@@ -280,6 +282,9 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+LAYOUTS = {"reference": 0, "compact": 1}  # CBQ_DAG_LAYOUT_*
+
+
 # ------------------------------------------------------------------ GPU arm
 
 def run_gpu(args, world, rank, local):
@@ -288,7 +293,7 @@ def run_gpu(args, world, rank, local):
 
     torch.cuda.set_device(local)
     nodes, root, batches, bounce = make_workload(args.workload)
-    dag = cbq.Dag(nodes, root)
+    dag = cbq.Dag(nodes, root, LAYOUTS[args.layout])
     kernel_id = {"auto": cbq.KERNEL_AUTO, "flat": cbq.KERNEL_FLAT, "nested": cbq.KERNEL_NESTED}[args.kernel]
     dag.set_launch_config(kernel_id, args.block, args.chunk if not args.persistent else 0, 0)
     cfg = dag.launch_config()
@@ -426,6 +431,7 @@ def run_gpu(args, world, rank, local):
                    "form": args.form, "launch_config": tuned if tuned else cfg,
                    "batches": {b[0]: int(b[1].shape[0]) for b in dev_batches},
                    "dag_nodes": int(dag.node_count), "dag_bytes": int(dag.bytes),
+                   "layout": args.layout, "device_node_bytes": int(dag.device_bytes),
                    "l2": "inputs larger than L2 (rays + hits %.0f MB per step); DAG read through L2"
                          % (rays_per_step * (RAY_BYTES + HIT_BYTES) / 1e6),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
@@ -505,7 +511,7 @@ def run_gpu_batch(args, world, rank, local):
 
     torch.cuda.set_device(local)
     host_jobs = batch_jobs()
-    dags = [cbq.Dag(n, r) for n, r, _, _ in host_jobs]
+    dags = [cbq.Dag(n, r, LAYOUTS[args.layout]) for n, r, _, _ in host_jobs]
     dev = [(torch.from_numpy(o).cuda(), torch.from_numpy(d).cuda()) for _, _, o, d in host_jobs]
     rays_per_step = sum(o.shape[0] for o, _ in dev)
     stream = torch.cuda.current_stream()
@@ -593,7 +599,8 @@ def run_gpu_batch(args, world, rank, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (64 seeded sphere/terrain volumes, edges 2^7..2^11, generated rays)",
         "config": {"workload": "batch-64", "volumes": len(dags), "rays_per_step": rays_per_step,
-                   "dag_bytes": int(sum(g.bytes for g in dags)), "batch_config": tuned,
+                   "dag_bytes": int(sum(g.bytes for g in dags)), "layout": args.layout,
+                   "device_node_bytes": int(sum(g.device_bytes for g in dags)), "batch_config": tuned,
                    "form": "one persistent launch replayed from a CUDA graph",
                    "l2": "inputs larger than L2 (rays + hits %.0f MB per step)" % (rays_per_step * 78 / 1e6)},
         "plain": {"value": plain_value, "unit": "Mrays/s", "ms_per_step": plain_ms / args.steps,

@@ -86,7 +86,7 @@ class LaunchConfig(ctypes.Structure):
 class _DagInfo(ctypes.Structure):
     _fields_ = [("node_count", ctypes.c_uint64), ("bytes", ctypes.c_uint64), ("root", ctypes.c_uint32),
                 ("max_subdag_height", ctypes.c_int32), ("subdags", SubDag * 8),
-                ("device_nodes", ctypes.c_void_p)]
+                ("device_nodes", ctypes.c_void_p), ("layout", ctypes.c_uint32), ("device_bytes", ctypes.c_uint64)]
 
 
 def _load() -> ctypes.CDLL:
@@ -117,6 +117,9 @@ _sig("cbq_abi_version", [], ctypes.c_int)
 _sig("cbq_dag_validate", [_P, _U64, _U32])
 _sig("cbq_find_subdags", [_P, _U64, _U32, ctypes.POINTER(SubDag)])
 _sig("cbq_dag_create", [_P, _U64, _U32, ctypes.POINTER(_P)])
+_sig("cbq_dag_create_ex", [_P, _U64, _U32, _U32, ctypes.POINTER(_P)])
+_sig("cbq_compact_store", [_P, _U64, _U32, ctypes.POINTER(ctypes.POINTER(ctypes.c_uint32)), ctypes.POINTER(_U64),
+                           ctypes.POINTER(_U32)])
 _sig("cbq_dag_destroy", [_P])
 _sig("cbq_dag_get_info", [_P, ctypes.POINTER(_DagInfo)])
 _sig("cbq_dag_set_l2_persistence", [_P, _P, ctypes.c_float])
@@ -225,6 +228,17 @@ def _take_malloced(ptr, count_words: int) -> np.ndarray:
     arr = np.ctypeslib.as_array(ptr, shape=(count_words,)).copy()
     _lib.cbq_free(ctypes.cast(ptr, ctypes.c_void_p))
     return arr
+
+
+def compact_store(nodes: np.ndarray, root: int) -> tuple[np.ndarray, list[int]]:
+    """The compact node store (LAYOUT_COMPACT) and the SubDAG root references in it."""
+    n = _nodes_arg(nodes)
+    p = ctypes.POINTER(ctypes.c_uint32)()
+    words = _U64()
+    refs = (_U32 * 8)()
+    _check(_lib.cbq_compact_store(_np_ptr(n), n.size // 8, root, ctypes.byref(p), ctypes.byref(words), refs),
+           "cbq_compact_store")
+    return _take_malloced(p, words.value), list(refs)
 
 
 def build_scene(kind: int, edge_log2: int, seed: int, param: int = 0, threads: int = 0) -> tuple[np.ndarray, int]:
@@ -336,12 +350,14 @@ class Query:
 
 
 class Dag:
-    """A DAG resident on the current CUDA device (cbq_dag)."""
+    """A DAG resident on the current CUDA device (cbq_dag).  layout selects the
+    device node store (LAYOUT_REFERENCE, or LAYOUT_COMPACT where possible;
+    see .layout)."""
 
-    def __init__(self, nodes: np.ndarray, root: int):
+    def __init__(self, nodes: np.ndarray, root: int, layout: int = 0):
         n = _nodes_arg(nodes)
         h = _P()
-        _check(_lib.cbq_dag_create(_np_ptr(n), n.size // 8, root, ctypes.byref(h)), "cbq_dag_create")
+        _check(_lib.cbq_dag_create_ex(_np_ptr(n), n.size // 8, root, layout, ctypes.byref(h)), "cbq_dag_create_ex")
         self._h = h
         info = _DagInfo()
         _check(_lib.cbq_dag_get_info(h, ctypes.byref(info)), "cbq_dag_get_info")
@@ -351,6 +367,8 @@ class Dag:
         self.max_subdag_height = info.max_subdag_height
         self.subdags = list(info.subdags)
         self.device_nodes = info.device_nodes
+        self.layout = info.layout
+        self.device_bytes = info.device_bytes
 
     @property
     def handle(self):
@@ -537,6 +555,8 @@ class _Request(ctypes.Structure):
                 ("ray_count", ctypes.c_uint64), ("query", _Query), ("host_hits", _Hits)]
 
 
+LAYOUT_REFERENCE = 0
+LAYOUT_COMPACT = 1
 SERVER_IN_PLACE = 0x1
 
 

@@ -38,7 +38,8 @@ def cache_key(dag: cbq.Dag, direction) -> str:
     import torch
     gpu = torch.cuda.get_device_name() if torch.cuda.is_available() else "cpu"
     size_class = int(round(math.log2(max(1, dag.bytes))))
-    return f"{gpu}|dag2^{size_class}|{ray_mix(direction)}"
+    layout = "|compact" if getattr(dag, "layout", 0) == cbq.LAYOUT_COMPACT else ""
+    return f"{gpu}|dag2^{size_class}{layout}|{ray_mix(direction)}"
 
 
 def _load() -> dict:

@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cstring>
 #include <new>
+#include <vector>
 
 using namespace cbq;
 
@@ -18,7 +19,7 @@ constexpr uint32_t kRefillDefault = 8;
 
 bool use_flat(const cbq_dag* dag)
 {
-    return dag->flat_ok && dag->cfg.kernel != CBQ_KERNEL_NESTED;
+    return dag->flat_ok && (dag->cfg.kernel != CBQ_KERNEL_NESTED || dag->layout == CBQ_DAG_LAYOUT_COMPACT);
 }
 
 int flat_block(const cbq_dag* dag) { return dag->cfg.block > 0 ? dag->cfg.block : kFlatBlockDefault; }
@@ -48,7 +49,7 @@ dev::DagParams make_dag_params(const cbq_dag* dag)
         p.sd[i].ly = dag->subdags[i].lower_bound[1];
         p.sd[i].lz = dag->subdags[i].lower_bound[2];
         p.sd[i].height = dag->subdags[i].node_height;
-        p.sd[i].node = dag->subdags[i].node_index;
+        p.sd[i].node = dag->sd_ref[i];
         p.sd[i].pad[0] = p.sd[i].pad[1] = p.sd[i].pad[2] = 0;
     }
     return p;
@@ -140,7 +141,13 @@ extern "C" {
 
 cbq_status cbq_dag_create(const uint32_t* host_nodes, uint64_t node_count, uint32_t root, cbq_dag** out)
 {
-    if (!out) return CBQ_ERR_INVALID_ARGUMENT;
+    return cbq_dag_create_ex(host_nodes, node_count, root, CBQ_DAG_LAYOUT_REFERENCE, out);
+}
+
+cbq_status cbq_dag_create_ex(const uint32_t* host_nodes, uint64_t node_count, uint32_t root, uint32_t layout,
+                             cbq_dag** out)
+{
+    if (!out || layout > CBQ_DAG_LAYOUT_COMPACT) return CBQ_ERR_INVALID_ARGUMENT;
     *out = nullptr;
     cbq_status st = validate_nodes(host_nodes, node_count, root);
     if (st != CBQ_OK) return st;
@@ -156,13 +163,33 @@ cbq_status cbq_dag_create(const uint32_t* host_nodes, uint64_t node_count, uint3
     for (int i = 0; i < 8; i++)
         if (dag->subdags[i].node_index > 0) dag->max_height = std::max(dag->max_height, dag->subdags[i].node_height);
     if (cudaGetDevice(&dag->device) != cudaSuccess) { delete dag; return CBQ_ERR_CUDA; }
-    const size_t bytes = (size_t)node_count * 32u;
+    for (int i = 0; i < 8; i++) dag->sd_ref[i] = dag->subdags[i].node_index;
+    const uint32_t* src = host_nodes;
+    size_t bytes = (size_t)node_count * 32u;
+    std::vector<uint32_t> compact;
+    if (layout == CBQ_DAG_LAYOUT_COMPACT) {
+        uint32_t refs[8];
+        const cbq_status cst = dag->flat_ok ? build_compact(host_nodes, node_count, dag->subdags, compact, refs)
+                                            : CBQ_ERR_INVALID_ARGUMENT;
+        if (cst == CBQ_OK) {
+            dag->layout = CBQ_DAG_LAYOUT_COMPACT;
+            std::memcpy(dag->sd_ref, refs, sizeof(refs));
+            src = compact.data();
+            bytes = compact.size() * sizeof(uint32_t);
+        } else {
+            cbq::log(CBQ_LOG_WARNING, "compact layout unavailable (%s): using the reference layout",
+                     dag->flat_ok ? "store beyond 128 MB" : "coordinates beyond 2^24");
+        }
+    }
+    dag->device_bytes = bytes;
     cudaError_t e = cudaMalloc((void**)&dag->d_nodes, bytes);
     if (e != cudaSuccess) { cudaGetLastError(); delete dag; return CBQ_ERR_OUT_OF_MEMORY; }
-    e = cudaMemcpy(dag->d_nodes, host_nodes, bytes, cudaMemcpyHostToDevice);
+    e = cudaMemcpy(dag->d_nodes, src, bytes, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) { cudaFree(dag->d_nodes); delete dag; return CBQ_ERR_CUDA; }
-    cbq::log(CBQ_LOG_INFO, "DAG uploaded to device %d: %llu nodes (%.1f MB), root %u, max sub-DAG height %d, %s kernel",
-             dag->device, (unsigned long long)node_count, bytes / 1e6, root, dag->max_height,
+    cbq::log(CBQ_LOG_INFO,
+             "DAG uploaded to device %d: %llu nodes, %s layout (%.1f MB), root %u, max sub-DAG height %d, %s kernel",
+             dag->device, (unsigned long long)node_count,
+             dag->layout == CBQ_DAG_LAYOUT_COMPACT ? "compact" : "reference", bytes / 1e6, root, dag->max_height,
              dag->flat_ok ? "flat" : "nested (coordinates beyond 2^24)");
     *out = dag;
     return CBQ_OK;
@@ -187,6 +214,8 @@ cbq_status cbq_dag_get_info(const cbq_dag* dag, cbq_dag_info* info)
     info->max_subdag_height = dag->max_height;
     std::memcpy(info->subdags, dag->subdags, sizeof(dag->subdags));
     info->device_nodes = dag->d_nodes;
+    info->layout = dag->layout;
+    info->device_bytes = dag->device_bytes;
     return CBQ_OK;
 }
 
@@ -202,8 +231,7 @@ cbq_status cbq_dag_set_l2_persistence(const cbq_dag* dag, cbq_stream_t stream, f
         if (max_window <= 0 || max_persist <= 0) return CBQ_OK;  // not supported: leave caching as is
         const size_t want = (size_t)((double)max_persist * fraction);
         if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want) != cudaSuccess) return CBQ_ERR_CUDA;
-        const size_t bytes = (size_t)dag->node_count * 32u;
-        const size_t window = std::min<size_t>(bytes, (size_t)max_window);
+        const size_t window = std::min<size_t>(dag->device_bytes, (size_t)max_window);
         attr.accessPolicyWindow.base_ptr = dag->d_nodes;
         attr.accessPolicyWindow.num_bytes = window;
         attr.accessPolicyWindow.hitRatio = (float)std::min(1.0, (double)want / (double)window);
@@ -244,6 +272,7 @@ cbq_status cbq_dag_set_launch_config(cbq_dag* dag, const cbq_launch_config* cfg)
     if (cfg->stack != CBQ_STACK_SHARED && cfg->stack != CBQ_STACK_LOCAL) return CBQ_ERR_INVALID_ARGUMENT;
     if (cfg->form < CBQ_FORM_PLAIN || cfg->form > CBQ_FORM_SORTED) return CBQ_ERR_INVALID_ARGUMENT;
     if (cfg->steps < 0 || cfg->steps > 8) return CBQ_ERR_INVALID_ARGUMENT;
+    if (cfg->kernel == CBQ_KERNEL_NESTED && dag->layout == CBQ_DAG_LAYOUT_COMPACT) return CBQ_ERR_INVALID_ARGUMENT;
     dag->cfg = *cfg;
     return CBQ_OK;
 }

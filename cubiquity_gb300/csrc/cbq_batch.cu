@@ -17,7 +17,9 @@
 namespace cbq {
 namespace dev {
 
+template <bool COMPACT>
 struct BatchSrc {
+    static constexpr bool kCompact = COMPACT;
     const JobDesc* __restrict__ jobs;
 
     __device__ __forceinline__ const QueryParams& query(const Lane& L) const { return jobs[L.job].q; }
@@ -35,7 +37,9 @@ struct BatchSrc {
 constexpr unsigned kFullMask = 0xffffffffu;
 
 // Descent stack in local memory and `steps` ESVO steps per loop iteration:
-// the faster choices for the single-volume kernel on GB300.
+// the faster choices for the single-volume kernel on GB300.  Every job of one
+// launch has the node store layout COMPACT.
+template <bool COMPACT>
 __global__ void __launch_bounds__(256) cbq_k_flat_batch(const JobDesc* __restrict__ jobs, uint32_t njobs,
                                                         uint64_t total, unsigned long long* __restrict__ counter,
                                                         uint32_t refill_min, uint32_t steps)
@@ -45,7 +49,7 @@ __global__ void __launch_bounds__(256) cbq_k_flat_batch(const JobDesc* __restric
     for (uint32_t j = threadIdx.x; j <= njobs; j += blockDim.x) prefix[j] = j < njobs ? jobs[j].first : total;
     __syncthreads();
 
-    BatchSrc c;
+    BatchSrc<COMPACT> c;
     c.jobs = jobs;
     const unsigned lane = threadIdx.x & 31u;
     const uint32_t below = (1u << lane) - 1u;
@@ -101,31 +105,42 @@ void fill_job_volume(dev::JobDesc& d, const cbq_dag* dag)
         d.sd[k].ly = s.lower_bound[1];
         d.sd[k].lz = s.lower_bound[2];
         d.sd[k].height = s.node_height;
-        d.sd[k].node = s.node_index;
+        d.sd[k].node = dag->sd_ref[k];
         d.sd[k].pad[0] = d.sd[k].pad[1] = d.sd[k].pad[2] = 0;
     }
 }
 
-cbq_status launch_batch_kernel(const dev::JobDesc* d_jobs, uint32_t njobs, uint64_t total, uint64_t* counter,
+namespace {
+
+template <bool COMPACT>
+cbq_status launch_batch_layout(const dev::JobDesc* d_jobs, uint32_t njobs, uint64_t total, uint64_t* counter,
                                int block, uint32_t refill, uint32_t steps, int device, cudaStream_t s)
 {
-    if (total == 0 || njobs == 0) return CBQ_OK;
-    if (steps == 0) steps = 1;
+    const auto kernel = dev::cbq_k_flat_batch<COMPACT>;
     if (cudaMemsetAsync(counter, 0, sizeof(uint64_t), s) != cudaSuccess) return CBQ_ERR_CUDA;
     const size_t smem = (size_t)(njobs + 1) * 8;  // the prefix offsets
     if (smem > 227u * 1024u) return CBQ_ERR_CAPACITY;
     if (smem > 48u * 1024u &&
-        cudaFuncSetAttribute(dev::cbq_k_flat_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-            cudaSuccess)
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return CBQ_ERR_CUDA;
     int sms = 0, per_sm = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return CBQ_ERR_CUDA;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::cbq_k_flat_batch, block, smem) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem) != cudaSuccess)
         return CBQ_ERR_CUDA;
     per_sm = std::max(per_sm, 1);
-    dev::cbq_k_flat_batch<<<sms * per_sm, block, smem, s>>>(d_jobs, njobs, total, (unsigned long long*)counter,
-                                                            refill, steps);
+    kernel<<<sms * per_sm, block, smem, s>>>(d_jobs, njobs, total, (unsigned long long*)counter, refill, steps);
     return cudaGetLastError() == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
+}
+
+}  // namespace
+
+cbq_status launch_batch_kernel(const dev::JobDesc* d_jobs, uint32_t njobs, uint64_t total, uint64_t* counter,
+                               int block, uint32_t refill, uint32_t steps, bool compact, int device, cudaStream_t s)
+{
+    if (total == 0 || njobs == 0) return CBQ_OK;
+    if (steps == 0) steps = 1;
+    return compact ? launch_batch_layout<true>(d_jobs, njobs, total, counter, block, refill, steps, device, s)
+                   : launch_batch_layout<false>(d_jobs, njobs, total, counter, block, refill, steps, device, s);
 }
 
 }  // namespace cbq
@@ -141,9 +156,11 @@ struct cbq_batch {
     int device = 0;
     std::vector<cbq_job> jobs;              // as given (host copy)
     std::vector<int> nested_jobs;           // jobs whose DAG needs the nested kernel
-    dev::JobDesc* d_jobs = nullptr;
+    dev::JobDesc* d_jobs = nullptr;         // reference-layout jobs, then compact-layout jobs
     uint32_t njobs = 0;                     // jobs in the device table
+    uint32_t njobs_ref = 0;                 // of which reference layout (one launch per layout)
     uint64_t total = 0;
+    uint64_t total_ref = 0;
     uint32_t steps = kBatchStepsDefault;
     uint64_t* d_counter = nullptr;
     cbq_query query{1, CBQ_MAX_FOOTPRINT_DISABLED, 0u, 0u};
@@ -161,8 +178,11 @@ cbq_status enqueue_batch(cbq_batch* b, cudaStream_t s)
         cbq_status st = cbq_intersect(jb.dag, &jb.rays, jb.ray_count, &b->query, &jb.hits, (cbq_stream_t)s);
         if (st != CBQ_OK) return st;
     }
-    return launch_batch_kernel(b->d_jobs, b->njobs, b->total, b->d_counter, b->block, b->refill, b->steps, b->device,
-                               s);
+    cbq_status st = launch_batch_kernel(b->d_jobs, b->njobs_ref, b->total_ref, b->d_counter, b->block, b->refill,
+                                        b->steps, false, b->device, s);
+    if (st != CBQ_OK) return st;
+    return launch_batch_kernel(b->d_jobs + b->njobs_ref, b->njobs - b->njobs_ref, b->total - b->total_ref,
+                               b->d_counter + 8, b->block, b->refill, b->steps, true, b->device, s);
 }
 
 void drop_graph(cbq_batch* b)
@@ -203,12 +223,12 @@ cbq_status cbq_batch_create(const cbq_job* jobs, int32_t job_count, const cbq_qu
     *out = nullptr;
     int device = 0;
     if (cudaGetDevice(&device) != cudaSuccess) return CBQ_ERR_CUDA;
-    std::vector<dev::JobDesc> table;
+    std::vector<dev::JobDesc> table, compact;
     cbq_batch* b = new (std::nothrow) cbq_batch();
     if (!b) return CBQ_ERR_OUT_OF_MEMORY;
     b->device = device;
     if (query) b->query = *query;
-    uint64_t first = 0;
+    uint64_t first = 0, first_compact = 0;
     for (int32_t j = 0; j < job_count; j++) {
         const cbq_job& jb = jobs[j];
         if (!jb.dag || jb.dag->device != device) { delete b; return CBQ_ERR_INVALID_ARGUMENT; }
@@ -233,16 +253,20 @@ cbq_status cbq_batch_create(const cbq_job* jobs, int32_t job_count, const cbq_qu
         d.out.normal = jb.hits.normal;
         d.out.voxel = jb.hits.voxel;
         d.out.status = jb.hits.status;
-        d.first = first;
+        const bool is_compact = jb.dag->layout == CBQ_DAG_LAYOUT_COMPACT;
+        d.first = is_compact ? first_compact : first;
         d.count = jb.ray_count;
         d.q.compute_surface = b->query.compute_surface;
         d.q.max_footprint = b->query.max_footprint;
         d.q.flags = b->query.flags;
-        table.push_back(d);
-        first += jb.ray_count;
+        (is_compact ? compact : table).push_back(d);
+        (is_compact ? first_compact : first) += jb.ray_count;
     }
+    b->njobs_ref = (uint32_t)table.size();
+    b->total_ref = first;
+    table.insert(table.end(), compact.begin(), compact.end());
     b->njobs = (uint32_t)table.size();
-    b->total = first;
+    b->total = first + first_compact;
     if (cudaMalloc((void**)&b->d_counter, 256 + table.size() * sizeof(dev::JobDesc)) != cudaSuccess) {
         cudaGetLastError();
         delete b;

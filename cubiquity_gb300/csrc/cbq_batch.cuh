@@ -30,10 +30,12 @@ struct JobDesc {
 void fill_job_volume(dev::JobDesc& d, const cbq_dag* dag);
 
 // Launches the persistent multi-volume kernel over `njobs` device-resident job
-// descriptors holding `total` rays, `steps` ESVO steps per loop iteration.
-// `counter` is zeroed on `stream` first.
+// descriptors holding `total` rays, `steps` ESVO steps per loop iteration; all
+// jobs' volumes have the compact layout, or none.  `counter` is zeroed on
+// `stream` first.
 cbq_status launch_batch_kernel(const dev::JobDesc* d_jobs, uint32_t njobs, uint64_t total, uint64_t* counter,
-                               int block, uint32_t refill, uint32_t steps, int device, cudaStream_t stream);
+                               int block, uint32_t refill, uint32_t steps, bool compact, int device,
+                               cudaStream_t stream);
 
 constexpr uint32_t kBatchStepsDefault = 4;
 

@@ -19,8 +19,9 @@ constexpr unsigned kFull = 0xffffffffu;
 // SHARED: descent stack in shared memory (one column per thread) or in a
 //         per-thread local array.
 // SORTED: ray g of the launch is ray perm[g] of the input (octant order).
-template <bool PERSISTENT, bool SHARED, bool SORTED>
-__global__ void __launch_bounds__(256) cbq_k_flat(FlatCtx c, uint64_t n, unsigned long long* __restrict__ counter,
+// Ctx: FlatCtxT of the node store layout.
+template <bool PERSISTENT, bool SHARED, bool SORTED, typename Ctx>
+__global__ void __launch_bounds__(256) cbq_k_flat(Ctx c, uint64_t n, unsigned long long* __restrict__ counter,
                                                   uint32_t refill_min, const uint32_t* __restrict__ perm,
                                                   uint32_t steps)
 {
@@ -143,25 +144,25 @@ bool float_positions_exact(const cbq_dag* dag)
 
 namespace {
 
-template <bool P, bool S, bool O>
-cbq_status launch_variant(const dev::FlatCtx& c, uint64_t n, const FlatLaunch& fl, int rows, cudaStream_t stream,
+template <bool P, bool S, bool O, typename Ctx>
+cbq_status launch_variant(const Ctx& c, uint64_t n, const FlatLaunch& fl, int rows, cudaStream_t stream,
                           int device)
 {
     const size_t smem = S ? (size_t)rows * fl.block * sizeof(uint32_t) : 0;
     if (!P) {
         const uint64_t blocks = (n + fl.block - 1) / fl.block;
         if (blocks > 0x7fffffffull) return CBQ_ERR_INVALID_ARGUMENT;
-        dev::cbq_k_flat<false, S, O><<<(unsigned)blocks, fl.block, smem, stream>>>(c, n, nullptr, 0u, fl.perm,
+        dev::cbq_k_flat<false, S, O, Ctx><<<(unsigned)blocks, fl.block, smem, stream>>>(c, n, nullptr, 0u, fl.perm,
                                                                                      fl.steps ? fl.steps : 1u);
     } else {
         int sms = 0, per_sm = 0;
         if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return CBQ_ERR_CUDA;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::cbq_k_flat<true, S, O>, fl.block, smem) !=
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::cbq_k_flat<true, S, O, Ctx>, fl.block, smem) !=
             cudaSuccess)
             return CBQ_ERR_CUDA;
         per_sm = std::max(per_sm, 1);
         if (cudaMemsetAsync(fl.counter, 0, sizeof(uint64_t), stream) != cudaSuccess) return CBQ_ERR_CUDA;
-        dev::cbq_k_flat<true, S, O><<<sms * per_sm, fl.block, smem, stream>>>(
+        dev::cbq_k_flat<true, S, O, Ctx><<<sms * per_sm, fl.block, smem, stream>>>(
             c, n, (unsigned long long*)fl.counter, fl.refill_min, fl.perm, fl.steps ? fl.steps : 1u);
     }
     return cudaGetLastError() == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
@@ -182,21 +183,10 @@ cbq_status launch_octant_sort(const float4* dir, uint64_t n, uint32_t* counts16,
     return cudaGetLastError() == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
 }
 
-cbq_status launch_flat(const cbq_dag* dag, const dev::DagParams& dp, const dev::QueryParams& q,
-                       const dev::HitsOut& out, const float4* orig, const float4* dir, uint64_t n,
-                       uint32_t* fetch_out, const FlatLaunch& fl, cudaStream_t stream)
+// The eight launch shapes of one context type.
+template <typename Ctx>
+cbq_status launch_ctx(const Ctx& c, uint64_t n, const FlatLaunch& fl, int rows, cudaStream_t stream, int dv)
 {
-    dev::FlatCtx c;
-    c.dag = dp;
-    c.q = q;
-    c.out = out;
-    c.orig = orig;
-    c.dir = dir;
-    c.fetch_out = fetch_out;
-    if (fl.persistent && !fl.counter) return CBQ_ERR_INVALID_ARGUMENT;
-    if (fl.perm && n >= 0xffffffffull) return CBQ_ERR_INVALID_ARGUMENT;
-    const int rows = std::max(1, (int)dag->max_height);
-    const int dv = dag->device;
     const bool sorted = fl.perm != nullptr;
     if (fl.persistent) {
         if (fl.local_stack)
@@ -210,6 +200,43 @@ cbq_status launch_flat(const cbq_dag* dag, const dev::DagParams& dp, const dev::
                       : launch_variant<false, false, false>(c, n, fl, rows, stream, dv);
     return sorted ? launch_variant<false, true, true>(c, n, fl, rows, stream, dv)
                   : launch_variant<false, true, false>(c, n, fl, rows, stream, dv);
+}
+
+template <typename Ctx>
+Ctx make_ctx(const dev::DagParams& dp, const dev::QueryParams& q, const dev::HitsOut& out, const float4* orig,
+             const float4* dir, uint32_t* fetch_out)
+{
+    Ctx c;
+    c.dag = dp;
+    c.q = q;
+    c.out = out;
+    c.orig = orig;
+    c.dir = dir;
+    c.fetch_out = fetch_out;
+    return c;
+}
+
+cbq_status launch_flat(const cbq_dag* dag, const dev::DagParams& dp, const dev::QueryParams& q,
+                       const dev::HitsOut& out, const float4* orig, const float4* dir, uint64_t n,
+                       uint32_t* fetch_out, const FlatLaunch& fl, cudaStream_t stream)
+{
+    if (fl.persistent && !fl.counter) return CBQ_ERR_INVALID_ARGUMENT;
+    if (fl.perm && n >= 0xffffffffull) return CBQ_ERR_INVALID_ARGUMENT;
+    const int rows = std::max(1, (int)dag->max_height);
+    const int dv = dag->device;
+    if (dag->layout == CBQ_DAG_LAYOUT_COMPACT) {
+        if (fetch_out) {  // load counting: one shape
+            using Ctx = dev::FlatCtxT<true, true>;
+            FlatLaunch one = fl;
+            one.persistent = false;
+            one.local_stack = true;
+            one.perm = nullptr;
+            return launch_variant<false, false, false>(make_ctx<Ctx>(dp, q, out, orig, dir, fetch_out), n, one, rows,
+                                                       stream, dv);
+        }
+        return launch_ctx(make_ctx<dev::FlatCtxT<true>>(dp, q, out, orig, dir, nullptr), n, fl, rows, stream, dv);
+    }
+    return launch_ctx(make_ctx<dev::FlatCtxT<false>>(dp, q, out, orig, dir, fetch_out), n, fl, rows, stream, dv);
 }
 
 }  // namespace cbq

@@ -38,6 +38,7 @@ struct Lane {
     int h, start_h;
     float last_exit;
     uint32_t fetches, status, mode;
+    uint32_t loads;              // node loads made (fetches minus skipped empty children)
     uint32_t job;                // batch kernel: index of the lane's job
     uint64_t ray;                // ray index within its job
     const uint32_t* nodes;       // batch kernel: the job's node store
@@ -45,8 +46,12 @@ struct Lane {
 
 // Where a lane's volume, rays and outputs are.  The lane functions below are
 // templates over this "source" so that the single-volume kernel and the
-// multi-volume batch kernel share the same arithmetic.
-struct FlatCtx {
+// multi-volume batch kernel share the same arithmetic.  COMPACT selects the
+// node store layout; COUNT_LOADS makes fetch_out receive node loads rather
+// than child probes (they differ only in the compact layout).
+template <bool COMPACT, bool COUNT_LOADS = false>
+struct FlatCtxT {
+    static constexpr bool kCompact = COMPACT;
     DagParams dag;
     QueryParams q;
     HitsOut out;
@@ -63,7 +68,7 @@ struct FlatCtx {
     __device__ __forceinline__ void write(const Lane& L, const RayResult& r) const
     {
         write_result(out, L.ray, r);
-        if (fetch_out) fetch_out[L.ray] = L.fetches;
+        if (fetch_out) fetch_out[L.ray] = COUNT_LOADS ? L.loads : L.fetches;
     }
 };
 
@@ -104,6 +109,7 @@ __device__ __forceinline__ void lane_begin(Lane& L, const Src& c, uint64_t i)
     if (L.ddy < 0.0f) { L.oct += 2u; L.ddy = __fadd_rn(L.ddy, FLT_MAX); }
     if (L.ddz < 0.0f) { L.oct += 4u; L.ddz = __fadd_rn(L.ddz, FLT_MAX); }
     L.fetches = 0u;
+    L.loads = 0u;
     L.status = kRayOk;
     L.mode = kLaneEnter;
 }
@@ -215,7 +221,7 @@ __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
         lane_finish(L, c, false, 0.0f, 0u, 0.0f, 0.0f, 0.0f);
         return;
     }
-    const uint32_t child = load_child(c.nodes(L), L.node, L.cid ^ L.sign);
+    const uint32_t child = child_of<Src::kCompact>(c.nodes(L), L.node, L.cid ^ L.sign, L.loads);
     L.fetches++;
     if (child > 0u) {
         const float c0x = (L.fx - L.rox) * L.ix;
@@ -240,7 +246,7 @@ __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
             uint32_t material = 0u;
             float nx = 0.0f, ny = 0.0f, nz = 0.0f;
             if (c.query(L).compute_surface) {
-                material = nearest_material(c.nodes(L), child, L.sign, L.fetches, L.status);
+                material = nearest_material<Src::kCompact>(c.nodes(L), child, L.sign, L.fetches, L.status, L.loads);
                 if (L.status != kRayOk) {
                     lane_finish(L, c, false, 0.0f, 0u, 0.0f, 0.0f, 0.0f);
                     return;

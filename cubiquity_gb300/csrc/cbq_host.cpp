@@ -103,6 +103,76 @@ cbq_status validate_heights(const uint32_t* nodes, uint64_t node_count, const cb
     return CBQ_OK;
 }
 
+cbq_status build_compact(const uint32_t* nodes, uint64_t node_count, const cbq_subdag subdags[8],
+                         std::vector<uint32_t>& store, uint32_t sd_ref[8])
+{
+    constexpr uint32_t kUnset = 0xffffffffu;
+    constexpr uint64_t kMaxUnits = 1ull << 24;
+    auto mask_of = [&](uint32_t n) {
+        uint32_t m = 0;
+        for (int k = 0; k < 8; k++)
+            if (nodes[(uint64_t)n * 8 + k] != 0u) m |= 1u << k;
+        return m;
+    };
+    // Internal nodes reachable from the SubDAG roots, breadth first (siblings
+    // and the hot upper levels end up next to each other).
+    std::vector<uint32_t> offset(node_count, kUnset);
+    std::vector<uint32_t> order;
+    uint64_t units = 1;  // unit 0 unused: every internal reference is >= 256
+    uint32_t material_root[kMaterialCount];
+    for (uint32_t m = 0; m < kMaterialCount; m++) material_root[m] = kUnset;
+    for (int k = 0; k < 8; k++) {
+        const uint32_t r = subdags[k].node_index;
+        if (r == 0u) {
+            sd_ref[k] = 0u;
+        } else if (r < kMaterialCount) {  // uniform octant: a node with eight children r
+            if (material_root[r] == kUnset) {
+                material_root[r] = (uint32_t)units;
+                units += 4;
+            }
+            sd_ref[k] = (material_root[r] << 8) | 0xffu;
+        } else if (offset[r] == kUnset) {
+            offset[r] = 0;  // queued
+            order.push_back(r);
+        }
+    }
+    for (size_t i = 0; i < order.size(); i++) {
+        const uint32_t n = order[i];
+        for (int k = 0; k < 8; k++) {
+            const uint32_t c = nodes[(uint64_t)n * 8 + k];
+            if (c >= kMaterialCount && offset[c] == kUnset) {
+                offset[c] = 0;
+                order.push_back(c);
+            }
+        }
+    }
+    for (const uint32_t n : order) {
+        if (units >= kMaxUnits) return CBQ_ERR_CAPACITY;  // offsets must fit 24 bits
+        offset[n] = (uint32_t)units;
+        units += (__builtin_popcount(mask_of(n)) + 1) / 2;
+    }
+    if (units > kMaxUnits) return CBQ_ERR_CAPACITY;
+    auto ref_of = [&](uint32_t c) { return c < kMaterialCount ? c : (offset[c] << 8) | mask_of(c); };
+    try {
+        store.assign(units * 2, 0u);
+    } catch (const std::bad_alloc&) {
+        return CBQ_ERR_OUT_OF_MEMORY;
+    }
+    for (uint32_t m = 1; m < kMaterialCount; m++)
+        if (material_root[m] != kUnset)
+            for (int k = 0; k < 8; k++) store[(uint64_t)material_root[m] * 2 + k] = m;
+    for (const uint32_t n : order) {
+        uint64_t w = (uint64_t)offset[n] * 2;
+        for (int k = 0; k < 8; k++) {
+            const uint32_t c = nodes[(uint64_t)n * 8 + k];
+            if (c != 0u) store[w++] = ref_of(c);
+        }
+    }
+    for (int k = 0; k < 8; k++)
+        if (subdags[k].node_index >= kMaterialCount) sd_ref[k] = ref_of(subdags[k].node_index);
+    return CBQ_OK;
+}
+
 }  // namespace cbq
 
 using namespace cbq;
@@ -152,6 +222,28 @@ cbq_status cbq_find_subdags(const uint32_t* nodes, uint64_t node_count, uint32_t
 }
 
 void cbq_free(void* p) { std::free(p); }
+
+cbq_status cbq_compact_store(const uint32_t* nodes, uint64_t node_count, uint32_t root, uint32_t** store,
+                             uint64_t* words, uint32_t subdag_refs[8])
+{
+    if (!store || !words || !subdag_refs) return CBQ_ERR_INVALID_ARGUMENT;
+    *store = nullptr;
+    *words = 0;
+    cbq_status st = validate_nodes(nodes, node_count, root);
+    if (st != CBQ_OK) return st;
+    cbq_subdag sd[8];
+    st = find_subdags(nodes, node_count, root, sd);
+    if (st == CBQ_OK) st = validate_heights(nodes, node_count, sd);
+    if (st != CBQ_OK) return st;
+    std::vector<uint32_t> v;
+    st = build_compact(nodes, node_count, sd, v, subdag_refs);
+    if (st != CBQ_OK) return st;
+    *store = (uint32_t*)std::malloc(v.size() * sizeof(uint32_t));
+    if (!*store) return CBQ_ERR_OUT_OF_MEMORY;
+    std::memcpy(*store, v.data(), v.size() * sizeof(uint32_t));
+    *words = v.size();
+    return CBQ_OK;
+}
 
 cbq_status cbq_dag_voxel(const uint32_t* nodes, uint64_t node_count, uint32_t root, int32_t x, int32_t y,
                          int32_t z, uint8_t* material)

@@ -6,6 +6,7 @@
 
 #include <cstdint>
 #include <mutex>
+#include <vector>
 
 namespace cbq {
 
@@ -27,11 +28,25 @@ void log(int level, const char* fmt, ...)
 // (which also excludes cycles), so a traversal never descends below the leaves.
 cbq_status validate_heights(const uint32_t* nodes, uint64_t node_count, const cbq_subdag subdags[8]);
 
+// Compact node store (CBQ_DAG_LAYOUT_COMPACT).  Every internal node reachable
+// from a SubDAG root keeps only its occupied children, packed in slot order.  A
+// reference to an internal node is (offset << 8) | occupancy mask, the offset
+// counted in 8-byte units from the start of the store; unit 0 is unused, so
+// every such reference is >= 256, above the material values, which children
+// keep as they are.  A SubDAG rooted at a material m becomes a node with eight
+// children m.  sd_ref[k] is SubDAG k's root reference (0 if empty).
+// CBQ_ERR_CAPACITY when the store would exceed 2^24 units (128 MB).
+cbq_status build_compact(const uint32_t* nodes, uint64_t node_count, const cbq_subdag subdags[8],
+                         std::vector<uint32_t>& store, uint32_t sd_ref[8]);
+
 }  // namespace cbq
 
 // The opaque DAG handle.
 struct cbq_dag {
-    uint32_t* d_nodes = nullptr;   // device, node_count * 8 words
+    uint32_t* d_nodes = nullptr;   // device: node_count * 8 words, or the compact store
+    uint32_t layout = CBQ_DAG_LAYOUT_REFERENCE;
+    uint64_t device_bytes = 0;     // size of the device node store
+    uint32_t sd_ref[8] = {};       // SubDAG roots as the device store refers to them
     uint64_t node_count = 0;
     uint32_t root = 0;
     cbq_subdag subdags[8];

@@ -259,7 +259,8 @@ cbq_status cbq_server::enqueue(Slot& s, const std::vector<Request*>& group)
             cudaSuccess)
             return CBQ_ERR_CUDA;
         cbq_status st = launch_batch_kernel(s.d_table, njobs, total, s.d_counter, cfg.block, cfg.refill_min,
-                                            kBatchStepsDefault, device, s.stream);
+                                            kBatchStepsDefault, group[0]->r.dag->layout == CBQ_DAG_LAYOUT_COMPACT,
+                                            device, s.stream);
         if (st != CBQ_OK) return st;
     }
     // Results back to the host.
@@ -292,6 +293,7 @@ void cbq_server::run_scheduler()
         while (!queue.empty() && group.size() < (size_t)cfg.max_batch_requests) {
             Request* rq = queue.front();
             if (!group.empty() && rays + rq->r.ray_count > cfg.max_batch_rays) break;
+            if (!group.empty() && rq->r.dag->layout != group[0]->r.dag->layout) break;  // one layout per launch
             uint64_t off = 0;
             if (rq->bytes && !pool.alloc(rq->bytes, &off)) break;  // FIFO: wait for memory rather than skip ahead
             rq->offset = off;

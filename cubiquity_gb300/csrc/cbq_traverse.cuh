@@ -72,6 +72,30 @@ __device__ __forceinline__ uint32_t load_child(const uint32_t* __restrict__ node
     return __ldg(nodes + ((size_t)node * 8u + slot));
 }
 
+// Child `slot` of node reference `node` in the compact store (the occupancy
+// mask is the reference's low byte, the packed children start at unit
+// node >> 8 of 8 bytes): an empty child costs no load.  `loads` counts loads.
+__device__ __forceinline__ uint32_t load_child_compact(const uint32_t* __restrict__ nodes, uint32_t node,
+                                                       uint32_t slot, uint32_t& loads)
+{
+    const uint32_t m = node & 0xffu;
+    if (!((m >> slot) & 1u)) return 0u;
+    loads++;
+    return __ldg(nodes + ((size_t)(node >> 8) * 2u + __popc(m & ((1u << slot) - 1u))));
+}
+
+template <bool COMPACT>
+__device__ __forceinline__ uint32_t child_of(const uint32_t* __restrict__ nodes, uint32_t node, uint32_t slot,
+                                             uint32_t& loads)
+{
+    if constexpr (COMPACT) {
+        return load_child_compact(nodes, node, slot, loads);
+    } else {
+        loads++;
+        return load_child(nodes, node, slot);
+    }
+}
+
 // Per-ray constants in the reflected frame.
 struct RayFrame {
     float ox, oy, oz;      // (origin + 0.5) * sign
@@ -126,13 +150,17 @@ struct EsvoOut {
 };
 
 // findNearestMaterial (raytracing.cpp:134-162).
+// `fetches` counts child probes (the reference's loads, which also bound the
+// walk); `loads` the loads actually made (fewer in the compact layout).
+template <bool COMPACT = false>
 __device__ __forceinline__ uint32_t nearest_material(const uint32_t* __restrict__ nodes, uint32_t node,
-                                                     uint32_t sign_bits, uint32_t& fetches, uint32_t& status)
+                                                     uint32_t sign_bits, uint32_t& fetches, uint32_t& status,
+                                                     uint32_t& loads)
 {
     const uint32_t order = (0x76534210u | 0x88888888u) ^ (sign_bits * 0x11111111u);
     while (node >= kMaterialCount) {
         for (uint32_t ids = order; ids != 0u; ids >>= 4) {
-            const uint32_t c = load_child(nodes, node, ids & 7u);
+            const uint32_t c = child_of<COMPACT>(nodes, node, ids & 7u, loads);
             fetches++;
             if (c > 0u) { node = c; break; }
         }
@@ -203,7 +231,8 @@ __device__ __forceinline__ EsvoOut esvo(const uint32_t* __restrict__ nodes, cons
                 res.hit = true;
                 res.distance = tce;
                 if (q.compute_surface) {
-                    res.material = nearest_material(nodes, child, f.sign_bits, fetches, status);
+                    uint32_t loads = 0;
+                    res.material = nearest_material(nodes, child, f.sign_bits, fetches, status, loads);
                     if (status != kRayOk) { res.hit = false; return res; }
                     const float sx = (f.sign_bits & 1u) ? 1.0f : -1.0f;  // -rayDirSign
                     const float sy = (f.sign_bits & 2u) ? 1.0f : -1.0f;

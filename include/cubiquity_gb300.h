@@ -93,6 +93,14 @@ typedef struct cbq_query {
 
 typedef struct cbq_dag cbq_dag;
 
+/* Device layouts of the node store.  REFERENCE is the reference's array as
+ * given (storage.h:51-116).  COMPACT keeps only occupied children, packed, and
+ * carries each internal node's 8-bit occupancy mask in the reference to it, so
+ * an empty child is known without a load; traversal decisions and results are
+ * identical. */
+#define CBQ_DAG_LAYOUT_REFERENCE 0u
+#define CBQ_DAG_LAYOUT_COMPACT 1u
+
 typedef struct cbq_dag_info {
     uint64_t node_count;      /* including the 256 material slots */
     uint64_t bytes;           /* node_count * 32 */
@@ -100,6 +108,8 @@ typedef struct cbq_dag_info {
     int32_t max_subdag_height;
     cbq_subdag subdags[8];
     const uint32_t* device_nodes;
+    uint32_t layout;          /* CBQ_DAG_LAYOUT_* in use */
+    uint64_t device_bytes;    /* bytes of the device node store */
 } cbq_dag_info;
 
 /* ---------------------------------------------------------------- basics */
@@ -133,6 +143,12 @@ cbq_status cbq_find_subdags(const uint32_t* nodes, uint64_t node_count, uint32_t
  * device path.  Synchronous. */
 cbq_status cbq_dag_create(const uint32_t* host_nodes, uint64_t node_count, uint32_t root,
                           cbq_dag** out);
+/* cbq_dag_create with a device layout (CBQ_DAG_LAYOUT_*; no reference
+ * counterpart).  COMPACT falls back to REFERENCE, with a log message, when the
+ * DAG needs the nested kernel (coordinates beyond +-2^24) or the compact store
+ * would exceed 128 MB; cbq_dag_get_info reports the layout in use. */
+cbq_status cbq_dag_create_ex(const uint32_t* host_nodes, uint64_t node_count, uint32_t root,
+                             uint32_t layout, cbq_dag** out);
 cbq_status cbq_dag_destroy(cbq_dag* dag);
 cbq_status cbq_dag_get_info(const cbq_dag* dag, cbq_dag_info* info);
 
@@ -418,6 +434,12 @@ cbq_status cbq_scene_voxels(cbq_scene_kind kind, int edge_log2, uint64_t seed, i
                             uint8_t* out);
 
 void cbq_free(void* p);
+
+/* The compact node store that CBQ_DAG_LAYOUT_COMPACT uploads (host only, for
+ * inspection and tests): *store (release with cbq_free) holds *words uint32;
+ * subdag_refs[k] is SubDAG k's root reference in it. */
+cbq_status cbq_compact_store(const uint32_t* nodes, uint64_t node_count, uint32_t root, uint32_t** store,
+                             uint64_t* words, uint32_t subdag_refs[8]);
 
 /* Volume::voxel (storage.cpp:481-499) on a host node array. */
 cbq_status cbq_dag_voxel(const uint32_t* nodes, uint64_t node_count, uint32_t root, int32_t x,
