@@ -271,7 +271,7 @@ cbq_status cbq_dag_set_launch_config(cbq_dag* dag, const cbq_launch_config* cfg)
     if (cfg->refill_min > 32) return CBQ_ERR_INVALID_ARGUMENT;
     if (cfg->stack != CBQ_STACK_SHARED && cfg->stack != CBQ_STACK_LOCAL) return CBQ_ERR_INVALID_ARGUMENT;
     if (cfg->form < CBQ_FORM_PLAIN || cfg->form > CBQ_FORM_SORTED) return CBQ_ERR_INVALID_ARGUMENT;
-    if (cfg->steps < 0 || cfg->steps > 8) return CBQ_ERR_INVALID_ARGUMENT;
+    if (cfg->steps < 0 || cfg->steps > 16) return CBQ_ERR_INVALID_ARGUMENT;
     if (cfg->kernel == CBQ_KERNEL_NESTED && dag->layout == CBQ_DAG_LAYOUT_COMPACT) return CBQ_ERR_INVALID_ARGUMENT;
     dag->cfg = *cfg;
     return CBQ_OK;
@@ -323,12 +323,12 @@ cbq_status cbq_autotune(cbq_dag* dag, const cbq_rays* rays, uint64_t n, const cb
     static const int blocks[] = {64, 128, 256};
     static const uint32_t refills[] = {4, 8, 16};
     static const int stacks[] = {CBQ_STACK_SHARED, CBQ_STACK_LOCAL};
-    static const int step_counts[] = {2, 4, 8};
+    static const int step_counts[] = {2, 4, 8, 16};
     for (int form = CBQ_FORM_PLAIN; form <= CBQ_FORM_SORTED && st == CBQ_OK; form++) {
         for (int blk : blocks) {
             for (uint32_t rf : refills) {
                 if (form == CBQ_FORM_PLAIN && rf != refills[0]) continue;  // refill unused
-                for (int stk_steps = 0; stk_steps < 6; stk_steps++) {
+                for (int stk_steps = 0; stk_steps < 8; stk_steps++) {
                     const int stk = stacks[stk_steps & 1];
                     cbq_launch_config c = saved;
                     c.kernel = dag->flat_ok ? CBQ_KERNEL_FLAT : CBQ_KERNEL_NESTED;

@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(256) cbq_k_flat_batch(const JobDesc* __restric
             continue;
         }
         lane_settle(L, c);
-        for (uint32_t k = 0; k < steps && L.mode == kLaneWalk; k++) lane_walk(L, c, stack);
+        lane_walk_steps(L, c, stack, steps);
     }
 }
 

@@ -37,6 +37,6 @@ cbq_status launch_batch_kernel(const dev::JobDesc* d_jobs, uint32_t njobs, uint6
                                int block, uint32_t refill, uint32_t steps, bool compact, int device,
                                cudaStream_t stream);
 
-constexpr uint32_t kBatchStepsDefault = 4;
+constexpr uint32_t kBatchStepsDefault = 8;
 
 }  // namespace cbq

@@ -63,12 +63,10 @@ __global__ void __launch_bounds__(256) cbq_k_flat(Ctx c, uint64_t n, unsigned lo
         lane_settle(L, c);
         // Up to `steps` ESVO steps per outer iteration: amortises the refill
         // ballot and the settle check over several node fetches.
-        for (uint32_t k = 0; k < steps && L.mode == kLaneWalk; k++) {
-            if (SHARED)
-                lane_walk(L, c, sstack);
-            else
-                lane_walk(L, c, lstack);
-        }
+        if (SHARED)
+            lane_walk_steps(L, c, sstack, steps);
+        else
+            lane_walk_steps(L, c, lstack, steps);
     }
 }
 

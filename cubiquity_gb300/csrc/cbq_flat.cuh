@@ -216,11 +216,6 @@ __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
     const float c1y = ((L.fy + L.fcns) - L.roy) * L.iy;
     const float c1z = ((L.fz + L.fcns) - L.roz) * L.iz;
     const float tcx = min3_ref(c1x, c1y, c1z);
-    if (L.fetches >= kMaxFetches) {
-        L.status = kRayIterLimit;
-        lane_finish(L, c, false, 0.0f, 0u, 0.0f, 0.0f, 0.0f);
-        return;
-    }
     const uint32_t child = child_of<Src::kCompact>(c.nodes(L), L.node, L.cid ^ L.sign, L.loads);
     L.fetches++;
     if (child > 0u) {
@@ -282,15 +277,33 @@ __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
         L.node = (L.written & (1u << h)) ? stack.get(h) : 0u;
         L.cns = (int32_t)(1u << msb);
         L.fcns = (float)L.cns;
-        L.cid = (uint32_t)((L.cx >> msb) & 1) | ((uint32_t)((L.cy >> msb) & 1) << 1) |
-                ((uint32_t)((L.cz >> msb) & 1) << 2);
-        L.cx = (int32_t)((uint32_t)(L.cx >> h) << h) + ((L.cid & 1u) ? L.cns : 0);
-        L.cy = (int32_t)((uint32_t)(L.cy >> h) << h) + ((L.cid & 2u) ? L.cns : 0);
-        L.cz = (int32_t)((uint32_t)(L.cz >> h) << h) + ((L.cid & 4u) ? L.cns : 0);
+        L.cid = (((uint32_t)L.cx >> msb) & 1u) | ((((uint32_t)L.cy >> msb) & 1u) << 1) |
+                ((((uint32_t)L.cz >> msb) & 1u) << 2);
+        const uint32_t keep = 0u - (uint32_t)L.cns;
+        L.cx = (int32_t)((uint32_t)L.cx & keep);
+        L.cy = (int32_t)((uint32_t)L.cy & keep);
+        L.cz = (int32_t)((uint32_t)L.cz & keep);
         L.fx = (float)L.cx;
         L.fy = (float)L.cy;
         L.fz = (float)L.cz;
         L.last_exit = 0.0f;
+    }
+}
+
+// Up to `steps` ESVO steps.  The reference ends a ray when a step starts with
+// the fetch budget spent (raytracing.cpp:253 with the cap): the steps here are
+// bounded by the budget left, and a lane still walking with the budget spent
+// ends exactly as that next step would have ended it.
+template <typename Src, typename Stack>
+__device__ __forceinline__ void lane_walk_steps(Lane& L, const Src& c, Stack& stack, uint32_t steps)
+{
+    if (L.mode != kLaneWalk) return;
+    const uint32_t budget = kMaxFetches - L.fetches;  // > 0: a walking lane is below the cap
+    const uint32_t n = steps < budget ? steps : budget;
+    for (uint32_t k = 0; k < n && L.mode == kLaneWalk; k++) lane_walk(L, c, stack);
+    if (L.mode == kLaneWalk && L.fetches >= kMaxFetches) {
+        L.status = kRayIterLimit;
+        lane_finish(L, c, false, 0.0f, 0u, 0.0f, 0.0f, 0.0f);
     }
 }
 

@@ -54,8 +54,8 @@ struct cbq_dag {
     int device = 0;
     bool flat_ok = false;          // float positions exact (coordinates within +-2^24)
     // Defaults from the GB300 sweep on terrain-4096 (primary and bounce rays):
-    // persistent refill, stack in local memory, 4 ESVO steps per loop iteration.
-    cbq_launch_config cfg{CBQ_KERNEL_AUTO, 0, 0, 0, CBQ_STACK_LOCAL, CBQ_FORM_PERSISTENT, 4, 0};
+    // persistent refill, stack in local memory, 8 ESVO steps per loop iteration.
+    cbq_launch_config cfg{CBQ_KERNEL_AUTO, 0, 0, 0, CBQ_STACK_LOCAL, CBQ_FORM_PERSISTENT, 8, 0};
 
     // Staging for cbq_intersect_host.
     std::mutex staging_lock;

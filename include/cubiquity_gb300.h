@@ -180,7 +180,7 @@ typedef struct cbq_launch_config {
     uint32_t refill_min;      /* flat persistent: idle lanes that trigger a refill, 0 = default */
     int32_t stack;            /* CBQ_STACK_* (flat kernel) */
     int32_t form;             /* CBQ_FORM_*, used by cbq_intersect_auto */
-    int32_t steps;            /* flat kernel: ESVO steps per loop iteration (1..8), 0 = 1 */
+    int32_t steps;            /* flat kernel: ESVO steps per loop iteration (1..16), 0 = 1 */
     int32_t reserved;
 } cbq_launch_config;
 
@@ -198,7 +198,7 @@ cbq_status cbq_intersect_auto(const cbq_dag* dag, const cbq_rays* rays, uint64_t
                               const cbq_hits* hits, void* scratch, uint64_t scratch_bytes, cbq_stream_t stream);
 
 /* Autotuner: times every form x block {64,128,256} x refill {4,8,16} x stack
- * {shared, local} x steps {2,4,8} on these rays (synchronous; `repetitions`
+ * {shared, local} x steps {2,4,8,16} on these rays (synchronous; `repetitions`
  * launches each),
  * stores the fastest in the DAG's launch config and returns it with its time. */
 cbq_status cbq_autotune(cbq_dag* dag, const cbq_rays* rays, uint64_t n, const cbq_query* query,

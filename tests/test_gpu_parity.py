@@ -261,3 +261,49 @@ def test_iteration_cap_on_malformed_dag(orc):
     got = _host(cbq.intersect_volume(dag, _dev(o), _dev(d), True, 0.5))
     assert (want["status"] == cbq.RAY_ITER_LIMIT).any()
     _assert_same(got, want, FIELDS + ("status",), what="iteration cap")
+
+
+def dotted_line_dag(height=20):
+    """Voxels at odd x on the line y = z = 0 of a 2^height volume at the
+    origin: one leaf node, then one node per level with two children."""
+    nodes = [np.repeat(np.arange(256, dtype=np.uint32), 8).reshape(256, 8)]
+    leaf = np.zeros(8, np.uint32)
+    leaf[1] = 1  # child (x=1, y=0, z=0): material 1
+    rows = [leaf]
+    for _ in range(height - 1):
+        r = np.zeros(8, np.uint32)
+        r[0] = r[1] = 256 + len(rows) - 1
+        rows.append(r)
+    for _ in range(31 - height):  # single-child chain up to height 31
+        r = np.zeros(8, np.uint32)
+        r[0] = 256 + len(rows) - 1
+        rows.append(r)
+    root = np.zeros(8, np.uint32)
+    root[7] = 256 + len(rows) - 1  # the octant x, y, z >= 0
+    rows.append(root)
+    nodes.append(np.stack(rows))
+    return np.concatenate(nodes).reshape(-1), 256 + len(rows) - 1
+
+
+def test_iteration_cap_inside_the_walk(orc):
+    """A ray grazing the line (in the voxel row y = 1) visits every leaf node along it
+    without a hit: more than 2^17 steps, so the walk itself reaches the fetch
+    cap and the ray ends with CBQ_RAY_ITER_LIMIT, in every kernel and layout."""
+    nodes, root = dotted_line_dag()
+    # Voxel v spans [v - 0.5, v + 0.5): rows y = 1 graze, y = 0 hits x = 1.
+    o = np.array([[-1.0, 1.0, 0.0, 0.0], [-1.0, 0.0, 0.0, 0.0], [-3.0, 1.25, -0.25, 0.0],
+                  [1000.0, 1.0, 0.0, 0.0]], np.float32)
+    d = np.array([[1.0, 1e-7, 1e-7, 0.0], [1.0, 1e-7, 1e-7, 0.0], [1.0, 2e-7, -1e-7, 0.0],
+                  [1.0, 1e-7, 1e-7, 0.0]], np.float32)
+    want = orc.intersect(nodes, orc.find_subdags(nodes, root), o, d)
+    assert want["status"].tolist() == [cbq.RAY_ITER_LIMIT, cbq.RAY_OK, cbq.RAY_ITER_LIMIT, cbq.RAY_ITER_LIMIT]
+    assert want["hit"].tolist() == [0, 1, 0, 0]
+    for layout in (cbq.LAYOUT_REFERENCE, cbq.LAYOUT_COMPACT):
+        dag = cbq.Dag(nodes, root, layout)
+        assert dag.layout == layout
+        for kernel in (cbq.KERNEL_FLAT, cbq.KERNEL_NESTED) if layout == cbq.LAYOUT_REFERENCE else (cbq.KERNEL_FLAT,):
+            for steps in (1, 3, 16):
+                dag.set_launch_config(kernel, 64, 0, 0, cbq.STACK_LOCAL, cbq.FORM_PERSISTENT, steps)
+                scratch = cbq.scratch_for(o.shape[0])
+                got = _host(cbq.intersect_auto(dag, _dev(o), _dev(d), scratch))
+                _assert_same(got, want, FIELDS + ("status",), what=f"layout {layout} kernel {kernel} steps {steps}")
