@@ -62,6 +62,8 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--layout", choices=["reference", "compact"], default="reference",
                    help="device node store: the reference's array, or the compact store (occupied children only)")
+    p.add_argument("--serve-inflight", type=int, default=8, help="serve-8: launches in flight")
+    p.add_argument("--serve-batch-rays", type=int, default=4 << 20, help="serve-8: rays per launch at most")
     p.add_argument("--serve-buffers", choices=["staged", "in-place"], default="staged",
                    help="serve-8: stage requests through device memory with copies, or traverse the page-locked "
                         "request buffers in place")
@@ -593,6 +595,7 @@ def run_gpu_batch(args, world, rank, local):
         dt = time.perf_counter() - t0
         cpu = {"value": rays_per_step / dt / 1e6, "unit": "Mrays/s", "cores": host_cores(), "kind": "port",
                "sample": f"one pass over all 64 volumes ({rays_per_step} rays), {host_cores()} host threads"}
+    batch_traffic = profiled_traffic("batch-64")  # DRAM bytes per ray, one launch (ncu)
     line = {
         "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": batched_ms / args.steps, "higher_is_better": True,
@@ -607,7 +610,10 @@ def run_gpu_batch(args, world, rank, local):
                   "form": "cbq_intersect once per volume (64 launches per step)"},
         "batched_over_plain": value / plain_value,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": f"{peak_kind} hbm_gbs", "kernel": "cbq_k_flat_batch", "traffic": None,
+                     "peak_source": f"{peak_kind} hbm_gbs", "kernel": "cbq_k_flat_batch",
+                     "traffic": None if batch_traffic is None else batch_traffic * rays_per_step,
+                     "limiter": {"kind": "instruction issue", "issue_active_pct": profiled_issue_active("batch-64"),
+                                 "source": "ncu --set full"},
                      "fetches_per_ray": fetches / rays_per_step,
                      "l2": {"stream_peak_gbs": l2_stream, "frac_stream": achieved / l2_stream,
                             "sector_rate_gsps": fetches / step_s / 1e9, "random_sector_peak_gsps": l2_rand}},
@@ -656,8 +662,8 @@ def run_gpu_serve(args, world, rank, local):
              "voxel": torch.empty((max_n, 3), dtype=torch.int32).pin_memory().numpy(),
              "status": torch.empty(max_n, dtype=torch.uint8).pin_memory().numpy()} for _ in range(ring)]
     in_place = args.serve_buffers == "in-place"
-    server = cbq.Server(device_memory_budget=2 << 30, max_inflight_launches=4, max_batch_requests=128,
-                        max_batch_rays=4 << 20, in_place=in_place)
+    server = cbq.Server(device_memory_budget=2 << 30, max_inflight_launches=args.serve_inflight,
+                        max_batch_requests=128, max_batch_rays=args.serve_batch_rays, in_place=in_place)
     queries = {True: cbq.Query(True, cbq.MAX_FOOTPRINT_DISABLED, True), False: cbq.Query()}
 
     def submit(k, r):
@@ -683,8 +689,8 @@ def run_gpu_serve(args, world, rank, local):
     n_peak = 3000
     # The same closed loop through a server of the other buffer mode.
     live = server
-    server = cbq.Server(device_memory_budget=2 << 30, max_inflight_launches=4, max_batch_requests=128,
-                        max_batch_rays=4 << 20, in_place=not in_place)
+    server = cbq.Server(device_memory_budget=2 << 30, max_inflight_launches=args.serve_inflight,
+                        max_batch_requests=128, max_batch_rays=args.serve_batch_rays, in_place=not in_place)
     closed_loop(0, 300)
     server.reset_stats()
     dt_other = closed_loop(300, n_peak)
@@ -701,7 +707,7 @@ def run_gpu_serve(args, world, rank, local):
 
     def open_loop(rate, duration, first):
         """Poisson arrivals at `rate` requests/s for `duration` seconds."""
-        rng = random.Random(rate)
+        rng = random.Random(rate * 1000.0 + first)
         times, t = [], 0.0
         while t < duration:
             t += rng.expovariate(rate)
@@ -739,8 +745,12 @@ def run_gpu_serve(args, world, rank, local):
 
     clocks = ClockSampler(local)
     clocks.start()
-    half = open_loop(0.5 * peak_rps, 4.0, 5000)
+    # Three 4 s runs at half load; the line reports the run with the median p99
+    # (host jitter from other work on the machine moves single-run tails).
+    halves = [open_loop(0.5 * peak_rps, 4.0, 5000 + 40000 * k) for k in range(3)]
     clk = clocks.stop()
+    half = dict(sorted(halves, key=lambda r: r["p99_ms"])[1])
+    half["p99_ms_runs"] = [r["p99_ms"] for r in halves]
     sweep = [open_loop(f * peak_rps, 2.0, 9000 + int(f * 1000)) for f in (0.25, 0.75)]
     server.close()
     line = {
@@ -749,7 +759,8 @@ def run_gpu_serve(args, world, rank, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (8 seeded terrain DAGs, 1k-256k-ray requests: 70% collision tmax<=64, 30% view)",
         "config": {"workload": "serve-8", "edges": [1 << s.edge_log2 for s in scenes],
-                   "server": {"memory_budget_gb": 2, "inflight_launches": 4, "max_batch_requests": 128,
+                   "server": {"memory_budget_gb": 2, "inflight_launches": args.serve_inflight,
+                              "max_batch_requests": 128, "max_batch_rays": args.serve_batch_rays,
                               "buffers": "page-locked host, served in place" if in_place else
                               "page-locked host, staged through device memory"},
                    "arrivals": "open-loop Poisson"},
