@@ -201,6 +201,10 @@ cbq_status cbq_dag_destroy(cbq_dag* dag)
     cudaFree(dag->d_nodes);
     if (dag->d_stage) cudaFree(dag->d_stage);
     if (dag->d_counter) cudaFree(dag->d_counter);
+    for (cudaStream_t& st : dag->pipe)
+        if (st) cudaStreamDestroy(st);
+    for (cudaEvent_t& ev : dag->pipe_ev)
+        if (ev) cudaEventDestroy(ev);
     delete dag;
     return CBQ_OK;
 }
@@ -437,17 +441,24 @@ cbq_status cbq_intersect_host(const cbq_dag* cdag, const float* host_origin_tmax
     if (n == 0) return CBQ_OK;
     cbq_dag* dag = const_cast<cbq_dag*>(cdag);
     std::lock_guard<std::mutex> lock(dag->staging_lock);
-    // Per ray: 32 B in, 46 B out (hit, distance, material, position, normal, voxel, status).
+    // Staging: rays (32 B), hit fields (46 B) per ray, then one work counter per chunk.
     const size_t per_ray = 32 + 1 + 4 + 4 + 12 + 12 + 12 + 1;
+    const size_t tail = 256 + kHostChunksMax * 64;
     if (n > dag->stage_capacity) {
         if (dag->d_stage) cudaFree(dag->d_stage);
         dag->d_stage = nullptr;
         dag->stage_capacity = 0;
-        if (cudaMalloc(&dag->d_stage, (size_t)n * per_ray + 256) != cudaSuccess) {
+        if (cudaMalloc(&dag->d_stage, (size_t)n * per_ray + tail) != cudaSuccess) {
             cudaGetLastError();
             return CBQ_ERR_OUT_OF_MEMORY;
         }
         dag->stage_capacity = n;
+    }
+    if (!dag->pipe[0]) {
+        for (int k = 0; k < 3; k++)
+            if (cudaStreamCreateWithFlags(&dag->pipe[k], cudaStreamNonBlocking) != cudaSuccess) return CBQ_ERR_CUDA;
+        for (int k = 0; k < 2 * kHostChunksMax; k++)
+            if (cudaEventCreateWithFlags(&dag->pipe_ev[k], cudaEventDisableTiming) != cudaSuccess) return CBQ_ERR_CUDA;
     }
     char* p = (char*)dag->d_stage;
     float* d_o = (float*)p;
@@ -463,34 +474,55 @@ cbq_status cbq_intersect_host(const cbq_dag* cdag, const float* host_origin_tmax
     dh.hit = (uint8_t*)p; p += n;
     dh.status = (uint8_t*)p;
     p += n;
-    // The persistent kernel's work counter: 8-byte aligned after the hit fields.
-    uint64_t* d_counter = (uint64_t*)(((uintptr_t)p + 7u) & ~(uintptr_t)7u);
-    cudaStream_t s = 0;
-    if (cudaMemcpyAsync(d_o, host_origin_tmax, n * 16, cudaMemcpyHostToDevice, s) != cudaSuccess) return CBQ_ERR_CUDA;
-    if (cudaMemcpyAsync(d_d, host_direction, n * 16, cudaMemcpyHostToDevice, s) != cudaSuccess) return CBQ_ERR_CUDA;
-    cbq_hits launch = dh;
-    if (!host_hits->hit) launch.hit = nullptr;
-    if (!host_hits->distance) launch.distance = nullptr;
-    if (!host_hits->material) launch.material = nullptr;
-    if (!host_hits->position) launch.position = nullptr;
-    if (!host_hits->normal) launch.normal = nullptr;
-    if (!host_hits->voxel) launch.voxel = nullptr;
-    if (!host_hits->status) launch.status = nullptr;
-    cbq_rays rays{d_o, d_d};
-    // Persistent form: its counter is private to this call (staging lock held).
-    cbq_status st = cbq_intersect_persistent(dag, &rays, n, query, &launch, d_counter, 0u, (cbq_stream_t)s);
-    if (st != CBQ_OK) return st;
-    struct Copy { void* dst; const void* src; size_t bytes; };
-    const Copy copies[] = {
-        {host_hits->hit, launch.hit, n}, {host_hits->distance, launch.distance, n * 4},
-        {host_hits->material, launch.material, n * 4}, {host_hits->position, launch.position, n * 12},
-        {host_hits->normal, launch.normal, n * 12}, {host_hits->voxel, launch.voxel, n * 12},
-        {host_hits->status, launch.status, n}};
-    for (const Copy& c : copies) {
-        if (!c.dst) continue;
-        if (cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess) return CBQ_ERR_CUDA;
+    // Work counters, one 64-byte line per chunk.
+    uint64_t* d_counters = (uint64_t*)(((uintptr_t)p + 255u) & ~(uintptr_t)255u);
+    // Chunks pipeline the copies with the traversal: while chunk k is traversed, chunk k + 1 is
+    // copied in and chunk k - 1 copied out (three streams ordered by events).
+    const uint64_t chunks = std::min<uint64_t>(kHostChunksMax, std::max<uint64_t>(1, n / kHostChunkMin));
+    const uint64_t per_chunk = (n + chunks - 1) / chunks;
+    cudaStream_t s_in = dag->pipe[0], s_run = dag->pipe[1], s_out = dag->pipe[2];
+    for (uint64_t k = 0; k * per_chunk < n; k++) {
+        const uint64_t a = k * per_chunk, m = std::min(per_chunk, n - a);
+        cudaEvent_t copied = dag->pipe_ev[2 * k], traversed = dag->pipe_ev[2 * k + 1];
+        if (cudaMemcpyAsync(d_o + 4 * a, host_origin_tmax + 4 * a, m * 16, cudaMemcpyHostToDevice, s_in) !=
+                cudaSuccess ||
+            cudaMemcpyAsync(d_d + 4 * a, host_direction + 4 * a, m * 16, cudaMemcpyHostToDevice, s_in) !=
+                cudaSuccess ||
+            cudaEventRecord(copied, s_in) != cudaSuccess || cudaStreamWaitEvent(s_run, copied, 0) != cudaSuccess)
+            return CBQ_ERR_CUDA;
+        cbq_hits launch;
+        launch.hit = host_hits->hit ? dh.hit + a : nullptr;
+        launch.distance = host_hits->distance ? dh.distance + a : nullptr;
+        launch.material = host_hits->material ? dh.material + a : nullptr;
+        launch.position = host_hits->position ? dh.position + 3 * a : nullptr;
+        launch.normal = host_hits->normal ? dh.normal + 3 * a : nullptr;
+        launch.voxel = host_hits->voxel ? dh.voxel + 3 * a : nullptr;
+        launch.status = host_hits->status ? dh.status + a : nullptr;
+        cbq_rays rays{d_o + 4 * a, d_d + 4 * a};
+        // Persistent form; each chunk's counter is private to this call (staging lock held).
+        cbq_status st = cbq_intersect_persistent(dag, &rays, m, query, &launch, d_counters + 8 * k, 0u,
+                                                 (cbq_stream_t)s_run);
+        if (st != CBQ_OK) return st;
+        if (cudaEventRecord(traversed, s_run) != cudaSuccess || cudaStreamWaitEvent(s_out, traversed, 0) != cudaSuccess)
+            return CBQ_ERR_CUDA;
+        struct Copy { void* dst; const void* src; size_t bytes; };
+        const Copy copies[] = {
+            {host_hits->hit ? host_hits->hit + a : nullptr, launch.hit, m},
+            {host_hits->distance ? host_hits->distance + a : nullptr, launch.distance, m * 4},
+            {host_hits->material ? host_hits->material + a : nullptr, launch.material, m * 4},
+            {host_hits->position ? host_hits->position + 3 * a : nullptr, launch.position, m * 12},
+            {host_hits->normal ? host_hits->normal + 3 * a : nullptr, launch.normal, m * 12},
+            {host_hits->voxel ? host_hits->voxel + 3 * a : nullptr, launch.voxel, m * 12},
+            {host_hits->status ? host_hits->status + a : nullptr, launch.status, m}};
+        for (const Copy& c : copies) {
+            if (!c.dst) continue;
+            if (cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToHost, s_out) != cudaSuccess)
+                return CBQ_ERR_CUDA;
+        }
     }
-    return cudaStreamSynchronize(s) == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
+    const bool ok = cudaStreamSynchronize(s_in) == cudaSuccess && cudaStreamSynchronize(s_run) == cudaSuccess &&
+                    cudaStreamSynchronize(s_out) == cudaSuccess;
+    return ok ? CBQ_OK : CBQ_ERR_CUDA;
 }
 
 }  // extern "C"

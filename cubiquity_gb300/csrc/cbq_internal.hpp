@@ -39,6 +39,11 @@ cbq_status validate_heights(const uint32_t* nodes, uint64_t node_count, const cb
 cbq_status build_compact(const uint32_t* nodes, uint64_t node_count, const cbq_subdag subdags[8],
                          std::vector<uint32_t>& store, uint32_t sd_ref[8]);
 
+// cbq_intersect_host splits a call into at most kHostChunksMax chunks of at
+// least kHostChunkMin rays.
+constexpr uint64_t kHostChunksMax = 8;
+constexpr uint64_t kHostChunkMin = 1ull << 18;
+
 }  // namespace cbq
 
 // The opaque DAG handle.
@@ -57,9 +62,12 @@ struct cbq_dag {
     // persistent refill, stack in local memory, 8 ESVO steps per loop iteration.
     cbq_launch_config cfg{CBQ_KERNEL_AUTO, 0, 0, 0, CBQ_STACK_LOCAL, CBQ_FORM_PERSISTENT, 8, 0};
 
-    // Staging for cbq_intersect_host.
+    // Staging for cbq_intersect_host: rays and hits, copied in and out in chunks on three
+    // streams (copy in, traverse, copy out) so that copies overlap the traversal.
     std::mutex staging_lock;
     void* d_stage = nullptr;
     uint64_t stage_capacity = 0;   // rays
     uint64_t* d_counter = nullptr;
+    struct CUstream_st* pipe[3] = {};  // cudaStream_t (this header is also compiled without CUDA)
+    struct CUevent_st* pipe_ev[2 * cbq::kHostChunksMax] = {};  // cudaEvent_t
 };

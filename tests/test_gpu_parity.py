@@ -172,6 +172,23 @@ def test_host_api_equals_device_api(terrain):
     _assert_same(c, {k: v[:1000] for k, v in a.items()}, FIELDS, what="host api reuse")
 
 
+@pytest.mark.parametrize("n", [(1 << 18) - 1, 3 * (1 << 18) + 17, 2_500_003])
+def test_host_api_chunks(terrain, n):
+    """Large host calls are split into chunks whose copies overlap the traversal
+    (one chunk per 2^18 rays, at most 8): every chunk size and boundary gives
+    the device path's bits, with all or some hit fields requested, from
+    pageable or page-locked buffers."""
+    nodes, root, dag, o, d = terrain
+    so, sd = _spread(o, n), _spread(d, n)
+    want = _host(cbq.intersect_volume(dag, _dev(so), _dev(sd), True, -1.0, use_tmax=True))
+    got = cbq.intersect_volume_host(dag, so, sd, use_tmax=True)
+    _assert_same(got, want, FIELDS + ("status",), what=f"host chunks {n}")
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
+    part = {k: pin(v) for k, v in cbq.alloc_host_hits(n).items() if k in ("hit", "voxel", "status")}
+    got = cbq.intersect_volume_host(dag, pin(so), pin(sd), use_tmax=True, out=part)
+    _assert_same(got, want, ("hit", "voxel", "status"), what=f"host chunks {n}, pinned, some fields")
+
+
 def test_fetch_counts_match_oracle(terrain, orc):
     nodes, root, dag, o, d = terrain
     n = 200_000
