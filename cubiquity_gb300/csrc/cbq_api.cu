@@ -455,7 +455,7 @@ cbq_status cbq_intersect_host(const cbq_dag* cdag, const float* host_origin_tmax
         dag->stage_capacity = n;
     }
     if (!dag->pipe[0]) {
-        for (int k = 0; k < 3; k++)
+        for (int k = 0; k < 4; k++)
             if (cudaStreamCreateWithFlags(&dag->pipe[k], cudaStreamNonBlocking) != cudaSuccess) return CBQ_ERR_CUDA;
         for (int k = 0; k < 2 * kHostChunksMax; k++)
             if (cudaEventCreateWithFlags(&dag->pipe_ev[k], cudaEventDisableTiming) != cudaSuccess) return CBQ_ERR_CUDA;
@@ -477,11 +477,15 @@ cbq_status cbq_intersect_host(const cbq_dag* cdag, const float* host_origin_tmax
     // Work counters, one 64-byte line per chunk.
     uint64_t* d_counters = (uint64_t*)(((uintptr_t)p + 255u) & ~(uintptr_t)255u);
     // Chunks pipeline the copies with the traversal: while chunk k is traversed, chunk k + 1 is
-    // copied in and chunk k - 1 copied out (three streams ordered by events).
+    // copied in and chunk k - 1 copied out.  Consecutive chunks are traversed on alternating
+    // streams, so the next chunk's blocks fill the SMs while the previous launch drains (a
+    // persistent launch ends with a tail of few busy warps).  Events order each chunk's copy in,
+    // traversal and copy out.
     const uint64_t chunks = std::min<uint64_t>(kHostChunksMax, std::max<uint64_t>(1, n / kHostChunkMin));
     const uint64_t per_chunk = (n + chunks - 1) / chunks;
-    cudaStream_t s_in = dag->pipe[0], s_run = dag->pipe[1], s_out = dag->pipe[2];
+    cudaStream_t s_in = dag->pipe[0], s_out = dag->pipe[1];
     for (uint64_t k = 0; k * per_chunk < n; k++) {
+        cudaStream_t s_run = dag->pipe[2 + (k & 1)];
         const uint64_t a = k * per_chunk, m = std::min(per_chunk, n - a);
         cudaEvent_t copied = dag->pipe_ev[2 * k], traversed = dag->pipe_ev[2 * k + 1];
         if (cudaMemcpyAsync(d_o + 4 * a, host_origin_tmax + 4 * a, m * 16, cudaMemcpyHostToDevice, s_in) !=
@@ -520,8 +524,8 @@ cbq_status cbq_intersect_host(const cbq_dag* cdag, const float* host_origin_tmax
                 return CBQ_ERR_CUDA;
         }
     }
-    const bool ok = cudaStreamSynchronize(s_in) == cudaSuccess && cudaStreamSynchronize(s_run) == cudaSuccess &&
-                    cudaStreamSynchronize(s_out) == cudaSuccess;
+    bool ok = true;
+    for (cudaStream_t st : dag->pipe) ok = cudaStreamSynchronize(st) == cudaSuccess && ok;
     return ok ? CBQ_OK : CBQ_ERR_CUDA;
 }
 

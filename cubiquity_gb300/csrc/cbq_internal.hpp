@@ -62,12 +62,12 @@ struct cbq_dag {
     // persistent refill, stack in local memory, 8 ESVO steps per loop iteration.
     cbq_launch_config cfg{CBQ_KERNEL_AUTO, 0, 0, 0, CBQ_STACK_LOCAL, CBQ_FORM_PERSISTENT, 8, 0};
 
-    // Staging for cbq_intersect_host: rays and hits, copied in and out in chunks on three
-    // streams (copy in, traverse, copy out) so that copies overlap the traversal.
+    // Staging for cbq_intersect_host: rays and hits, copied in and out in chunks on four
+    // streams (copy in, copy out, two for traversal) so that copies overlap the traversal.
     std::mutex staging_lock;
     void* d_stage = nullptr;
     uint64_t stage_capacity = 0;   // rays
     uint64_t* d_counter = nullptr;
-    struct CUstream_st* pipe[3] = {};  // cudaStream_t (this header is also compiled without CUDA)
+    struct CUstream_st* pipe[4] = {};  // cudaStream_t (this header is also compiled without CUDA)
     struct CUevent_st* pipe_ev[2 * cbq::kHostChunksMax] = {};  // cudaEvent_t
 };
