@@ -40,6 +40,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 HIT_BYTES = 1 + 4 + 4 + 12 + 12 + 12 + 1  # hit, distance, material, position, normal, voxel, status
+REF_HIT_BYTES = 1 + 4 + 4 + 12 + 12  # the reference's result fields only
 RAY_BYTES = 32
 SECTOR = 32
 
@@ -395,13 +396,13 @@ def run_gpu(args, world, rank, local):
         po = torch.from_numpy(o).pin_memory()
         pd = torch.from_numpy(d).pin_memory()
         n = o.shape[0]
+        # The reference's RayVolumeIntersection fields (raytracing.h:48-55): what a drop-in
+        # caller receives.  voxel and status are extra outputs it does not have.
         outs = {"hit": torch.empty(n, dtype=torch.uint8).pin_memory(),
                 "distance": torch.empty(n, dtype=torch.float32).pin_memory(),
                 "material": torch.empty(n, dtype=torch.int32).pin_memory(),
                 "position": torch.empty((n, 3), dtype=torch.float32).pin_memory(),
-                "normal": torch.empty((n, 3), dtype=torch.float32).pin_memory(),
-                "voxel": torch.empty((n, 3), dtype=torch.int32).pin_memory(),
-                "status": torch.empty(n, dtype=torch.uint8).pin_memory()}
+                "normal": torch.empty((n, 3), dtype=torch.float32).pin_memory()}
         host.append((po.numpy(), pd.numpy(), {k: v.numpy() for k, v in outs.items()}))
 
     def e2e_step():
@@ -443,7 +444,9 @@ def run_gpu(args, world, rank, local):
         "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": rays_per_step * RAY_BYTES,
-                "d2h_bytes_per_step": rays_per_step * HIT_BYTES},
+                "d2h_bytes_per_step": rays_per_step * REF_HIT_BYTES,
+                "api": "cbq_intersect_host (pinned host buffers, copies pipelined with the traversal inside)",
+                "fields": "hit, distance, material, position, normal (the reference's RayVolumeIntersection)"},
         "gpu_launches": launches,
         "clocks": clk,
     }
@@ -741,7 +744,8 @@ def run_gpu_serve(args, world, rank, local):
         return {"rate_rps": rate, "requests": len(times), "p50_ms": st["latency_p50_us"] / 1e3,
                 "p99_ms": st["latency_p99_us"] / 1e3, "max_ms": st["latency_max_us"] / 1e3,
                 "mrays_per_s": st["rays_completed"] / wall / 1e6, "requests_per_launch": st["mean_requests_per_launch"],
-                "generator_backpressure": backpressure, "direct_requests": st["direct_requests"]}
+                "generator_backpressure": backpressure, "direct_requests": st["direct_requests"],
+                "launches": st["launches"]}
 
     clocks = ClockSampler(local)
     clocks.start()
@@ -771,7 +775,7 @@ def run_gpu_serve(args, world, rank, local):
                                "p50_ms": other["latency_p50_us"] / 1e3, "p99_ms": other["latency_p99_us"] / 1e3},
         "half_load": half, "sweep": sweep,
         "e2e": {"value": half["mrays_per_s"], "unit": "Mrays/s", "note": "host rays in, host hits out, per request"},
-        "gpu_launches": None, "clocks": clk,
+        "gpu_launches": half["launches"], "clocks": clk,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -823,11 +827,13 @@ def run_gpu_city(args, world, rank, local):
     clocks.start()
     barrier(world)
     rays = 0
+    launches = 0
     ms = []
     t0 = time.perf_counter()
     for k in range(args.steps):
         img, st = cbq.pathtrace(dag, w, h, spp, bounces, eye, target, mats, seed=100 + k)
         rays += st["extension_rays"] + st["shadow_rays"]
+        launches += st["kernel_launches"]
         ms.append(st["milliseconds"])
     wall = max_over_ranks(world, time.perf_counter() - t0)
     clk = clocks.stop()
@@ -843,7 +849,7 @@ def run_gpu_city(args, world, rank, local):
         "verification": {"frame": "1 spp, 1920x1080, 4 bounces", "traversals_checked": checked,
                          "mismatches": mismatched, "oracle_seconds": cpu_s},
         "e2e": {"value": value, "unit": "Mrays/s", "note": "camera rays generated on the device; image stays there"},
-        "gpu_launches": None, "clocks": clk,
+        "gpu_launches": launches, "clocks": clk,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

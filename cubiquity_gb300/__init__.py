@@ -673,7 +673,7 @@ class _PtConfig(ctypes.Structure):
 
 class _PtStats(ctypes.Structure):
     _fields_ = [("extension_rays", ctypes.c_uint64), ("shadow_rays", ctypes.c_uint64),
-                ("milliseconds", ctypes.c_double)]
+                ("milliseconds", ctypes.c_double), ("kernel_launches", ctypes.c_uint64)]
 
 
 PT_WAVE_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
@@ -740,7 +740,7 @@ def pathtrace(dag: Dag, width: int, height: int, samples_per_pixel: int, bounces
     _check(_lib.cbq_pathtrace(dag.handle, ctypes.byref(cfg), image.data_ptr(), cb, None, ctypes.byref(stats),
                               _stream_ptr(stream)), "cbq_pathtrace")
     return image, {"extension_rays": stats.extension_rays, "shadow_rays": stats.shadow_rays,
-                   "milliseconds": stats.milliseconds}
+                   "milliseconds": stats.milliseconds, "kernel_launches": stats.kernel_launches}
 
 
 # ------------------------------------------------------------ batched form

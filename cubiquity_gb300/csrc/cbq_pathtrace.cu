@@ -298,7 +298,7 @@ extern "C" cbq_status cbq_pathtrace(const cbq_dag* dag, const cbq_pt_config* cfg
     }
 
     cbq_status st = CBQ_OK;
-    uint64_t ext_rays = 0, shadow_rays = 0;
+    uint64_t ext_rays = 0, shadow_rays = 0, launches = 0;
     auto fail = [&](cbq_status code) {
         st = code;
         cudaGetLastError();
@@ -324,6 +324,7 @@ extern "C" cbq_status cbq_pathtrace(const cbq_dag* dag, const cbq_pt_config* cfg
         fr.tan_half = (float)cfg->tan_half_fov;
         fr.aspect = (float)cfg->width / (float)cfg->height;
         cbq_k_pt_camera<<<(unsigned)((npix + 255) / 256), 256, 0, s>>>(fr, e[0].o, e[0].d, e[0].st);
+        launches++;
         uint32_t n = (uint32_t)npix;
         int cur = 0;
         for (int depth = 0; depth <= cfg->bounces && n > 0 && st == CBQ_OK; depth++) {
@@ -334,6 +335,7 @@ extern "C" cbq_status cbq_pathtrace(const cbq_dag* dag, const cbq_pt_config* cfg
             cbq_status ts = cbq_intersect_persistent(dag, &rays, n, &qext, &hits, work, 0u, (cbq_stream_t)s);
             if (ts != CBQ_OK) { fail(ts); break; }
             ext_rays += n;
+            launches++;
             if (on_wave) {
                 if (cudaStreamSynchronize(s) != cudaSuccess) { fail(CBQ_ERR_CUDA); break; }
                 on_wave(user, 0, depth, sample, (const float*)E.o, (const float*)E.d, n, &hits, &qext);
@@ -343,6 +345,7 @@ extern "C" cbq_status cbq_pathtrace(const cbq_dag* dag, const cbq_pt_config* cfg
             cbq_k_pt_shade<<<(n + 255) / 256, 256, 0, s>>>(d_sh, n, (uint32_t)depth, (uint32_t)sample, cfg->seed, last,
                                                           E.st, E.hit, E.material, E.position, E.normal, device_image,
                                                           so, sd, sw, counters, N.o, N.d, N.st, counters + 1);
+            launches++;
             uint32_t h_counts[2] = {0, 0};
             if (cudaMemcpyAsync(h_counts, counters, sizeof(h_counts), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
                 cudaStreamSynchronize(s) != cudaSuccess) {
@@ -356,11 +359,13 @@ extern "C" cbq_status cbq_pathtrace(const cbq_dag* dag, const cbq_pt_config* cfg
                 ts = cbq_intersect_persistent(dag, &srays, ns, &qsh, &shits, work + 1, 0u, (cbq_stream_t)s);
                 if (ts != CBQ_OK) { fail(ts); break; }
                 shadow_rays += ns;
+                launches++;
                 if (on_wave) {
                     if (cudaStreamSynchronize(s) != cudaSuccess) { fail(CBQ_ERR_CUDA); break; }
                     on_wave(user, 1, depth, sample, (const float*)so, (const float*)sd, ns, &shits, &qsh);
                 }
                 cbq_k_pt_shadow_add<<<(ns + 255) / 256, 256, 0, s>>>(ns, shit, sw, device_image);
+                launches++;
             }
             n = h_counts[1];
             cur ^= 1;
@@ -370,12 +375,14 @@ extern "C" cbq_status cbq_pathtrace(const cbq_dag* dag, const cbq_pt_config* cfg
         const size_t cnt = npix * 3;
         cbq_k_pt_scale<<<(unsigned)((cnt + 255) / 256), 256, 0, s>>>(device_image, cnt,
                                                                        1.0f / (float)cfg->samples_per_pixel);
+        launches++;
         if (cudaStreamSynchronize(s) != cudaSuccess) fail(CBQ_ERR_CUDA);
     }
     cudaFree(base);
     if (stats) {
         stats->extension_rays = ext_rays;
         stats->shadow_rays = shadow_rays;
+        stats->kernel_launches = launches;
         stats->milliseconds =
             std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
     }

@@ -384,6 +384,7 @@ typedef struct cbq_pt_config {
 typedef struct cbq_pt_stats {
     uint64_t extension_rays, shadow_rays;
     double milliseconds;
+    uint64_t kernel_launches;       /* kernels of this library launched for the frame */
 } cbq_pt_stats;
 
 /* Called after every traversal wave with device pointers to its rays and hits
