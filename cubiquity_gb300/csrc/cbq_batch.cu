@@ -322,33 +322,38 @@ cbq_status cbq_batch_autotune(cbq_batch* b, cbq_stream_t stream, int32_t repetit
     if (!b || repetitions <= 0) return CBQ_ERR_INVALID_ARGUMENT;
     static const int blocks[] = {64, 128, 256};
     static const uint32_t refills[] = {4, 8, 12, 16};
+    static const uint32_t step_counts[] = {4, 8, 16};
     cudaEvent_t e0, e1;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return CBQ_ERR_CUDA;
     float best = 1e30f;
     int best_block = b->block;
-    uint32_t best_refill = b->refill;
+    uint32_t best_refill = b->refill, best_steps = b->steps;
     cbq_status st = CBQ_OK;
-    for (int blk : blocks) {
-        for (uint32_t rf : refills) {
-            b->block = blk;
-            b->refill = rf;
-            st = enqueue_batch(b, (cudaStream_t)stream);  // warm-up
-            if (st != CBQ_OK) break;
-            cudaEventRecord(e0, (cudaStream_t)stream);
-            for (int r = 0; r < repetitions && st == CBQ_OK; r++) st = enqueue_batch(b, (cudaStream_t)stream);
-            cudaEventRecord(e1, (cudaStream_t)stream);
-            if (st != CBQ_OK || cudaEventSynchronize(e1) != cudaSuccess) { st = CBQ_ERR_CUDA; break; }
-            float ms = 0;
-            cudaEventElapsedTime(&ms, e0, e1);
-            if (ms < best) { best = ms; best_block = blk; best_refill = rf; }
-        }
+    for (int k = 0; k < 3 * 4 * 3 && st == CBQ_OK; k++) {
+        const int blk = blocks[k / 12];
+        const uint32_t rf = refills[(k / 3) % 4];
+        b->block = blk;
+        b->refill = rf;
+        b->steps = step_counts[k % 3];
+        st = enqueue_batch(b, (cudaStream_t)stream);  // warm-up
         if (st != CBQ_OK) break;
+        cudaEventRecord(e0, (cudaStream_t)stream);
+        for (int r = 0; r < repetitions && st == CBQ_OK; r++) st = enqueue_batch(b, (cudaStream_t)stream);
+        cudaEventRecord(e1, (cudaStream_t)stream);
+        if (st != CBQ_OK || cudaEventSynchronize(e1) != cudaSuccess) { st = CBQ_ERR_CUDA; break; }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) { best = ms; best_block = blk; best_refill = rf; best_steps = b->steps; }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     b->block = best_block;
     b->refill = best_refill;
+    b->steps = best_steps;
     drop_graph(b);
+    if (st == CBQ_OK)
+        cbq::log(CBQ_LOG_INFO, "batch autotune: block %d, refill %u, %u steps per iteration: %.3f ms per launch",
+                 best_block, best_refill, best_steps, best / (float)repetitions);
     return st;
 }
 
