@@ -1,0 +1,51 @@
+"""Randomised parity: random small DAGs (spheres, boxes, uniform and empty
+octants, noise, one to six materials) at random places, random rays (inside
+and outside, axis-aligned, diagonal, on voxel faces), every query; the CUDA
+path in both node layouts and both kernels against the oracle, bit for bit."""
+import numpy as np
+import pytest
+
+import cubiquity_gb300 as cbq
+import oracle
+from dagbuild import build_dag, random_voxels, random_rays
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+FIELDS = ("hit", "distance", "material", "position", "normal", "voxel", "status")
+QUERIES = [(True, -1.0, False), (False, -1.0, False), (True, 0.02, False), (True, 0.3, False), (True, -1.0, True)]
+
+
+def _same(got, want, what):
+    for k in FIELDS:
+        g = got[k].cpu().numpy()
+        w = want[k]
+        if k == "material":
+            g, w = g.astype(np.uint32), w.astype(np.uint32)
+        if not oracle.same_bits_nan_equal(g, w):
+            bad = np.nonzero((g != w).reshape(g.shape[0], -1).any(axis=1))[0]
+            raise AssertionError(f"{what}: {k} differs on {bad.size} rays, first {bad[:8].tolist()}")
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_random_dag_parity(seed, orc):
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(1000 + seed)
+    edge = 1 << int(rng.integers(2, 7))
+    vox = random_voxels(rng, edge)
+    span = (1 << 30) if seed % 6 == 5 else (1 << 21)  # every sixth volume needs the nested kernel
+    origin = tuple(int(x) * edge for x in rng.integers(-span // edge, span // edge, 3))
+    nodes, root = build_dag(vox, origin)
+    o, d = random_rays(rng, origin, edge, 4000)
+    sd = orc.find_subdags(nodes, root)
+    dags = {"reference": cbq.Dag(nodes, root), "compact": cbq.Dag(nodes, root, cbq.LAYOUT_COMPACT)}
+    to, td = torch.from_numpy(o).cuda(), torch.from_numpy(d).cuda()
+    for cs, mf, tmax in QUERIES:
+        want = orc.intersect(nodes, sd, o, d, cs, mf, use_tmax=tmax)
+        for name, dag in dags.items():
+            kernels = [cbq.KERNEL_AUTO] + ([cbq.KERNEL_NESTED] if name == "reference" else [])
+            for kernel in kernels:
+                dag.set_launch_config(kernel)
+                got = cbq.intersect_volume(dag, to, td, cs, mf, use_tmax=tmax)
+                _same(got, want, f"seed {seed} edge {edge} origin {origin} {name} kernel {kernel} "
+                                 f"query {(cs, mf, tmax)}")

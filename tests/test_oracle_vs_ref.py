@@ -126,3 +126,40 @@ def test_we_read_dag_files_the_reference_writes(ref, tmp_path):
     vol.save(p)
     nodes, root = cbq.load_dag(p)
     assert root == vol.root and np.array_equal(nodes, vol.nodes())
+
+
+@pytest.mark.reference
+@pytest.mark.parametrize("seed", range(8))
+def test_random_dags_oracle_equals_reference(ref, orc, seed):
+    """Random voxel sets at random places (tests/dagbuild.py): the reference's
+    setVoxel + bake gives the graph the test builder gives, and the oracle
+    gives the reference's results on random rays (those the oracle finishes
+    with status OK and that read no never-written stack slot)."""
+    from dagbuild import build_dag, random_voxels, random_rays as rays_for
+    rng = np.random.default_rng(5000 + seed)
+    edge = 1 << int(rng.integers(2, 6))
+    vox = random_voxels(rng, edge)
+    origin = tuple(int(x) * edge for x in rng.integers(-(1 << 12) // edge, (1 << 12) // edge, 3))
+    nodes, root = build_dag(vox, origin)
+    vol = ref.new_volume()
+    zz, yy, xx = np.nonzero(vox)
+    if zz.size:
+        vol.set_voxels(np.stack([xx + origin[0], yy + origin[1], zz + origin[2]], 1), vox[zz, yy, xx])
+    vol.bake()
+    assert cbq.canonical_hash(nodes, root) == cbq.canonical_hash(vol.nodes(), vol.root)
+    sd = vol.find_subdags()
+    assert sd == orc.find_subdags(vol.nodes(), vol.root)
+    assert [s[:2] for s in sd] == [s[:2] for s in orc.find_subdags(nodes, root)]  # node numbering differs
+    o, d = rays_for(rng, origin, edge, 3000)
+    o[:, 3] = np.inf
+    for query in [(True, -1.0), (False, -1.0), (True, 0.05)]:
+        b = orc.intersect(vol.nodes(), sd, o, d, *query)
+        ok = b["status"] == 0
+        undefined = oracle.undefined_stack_rays(orc, vol.nodes(), sd, o, d, compute_surface=query[0],
+                                                max_footprint=query[1])
+        ok[undefined] = False
+        assert ok.sum() > 0.9 * o.shape[0]
+        a = vol.intersect(sd, o[ok], d[ok], *query)
+        for k in FIELDS + ("distance",):
+            want = a[k].astype(np.float32) if k == "distance" else a[k]
+            assert oracle.same_bits_nan_equal(want, b[k][ok]), (query, k)
