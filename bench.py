@@ -243,6 +243,21 @@ def cpu_trace(nodes, root, batches, threads=0):
     return time.perf_counter() - t0, "port"
 
 
+def host_cpu() -> str:
+    """The host CPU's model (for the CPU baseline record)."""
+    import platform
+    try:
+        info = Path("/proc/cpuinfo").read_text()
+    except OSError:
+        return platform.machine()
+    m = re.search(r"^model name\s*:\s*(.+)$", info, re.M)
+    if m:
+        return m.group(1).strip()
+    part = re.search(r"^CPU part\s*:\s*(\S+)$", info, re.M)
+    names = {"0xd4f": "Arm Neoverse V2 (NVIDIA Grace)"}
+    return names.get(part.group(1), f"{platform.machine()} CPU part {part.group(1)}") if part else platform.machine()
+
+
 def host_cores() -> int:
     try:
         return len(os.sched_getaffinity(0))
@@ -277,7 +292,7 @@ def run_reference(args, world, rank):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene, generated rays)",
         "impl": "reference",
         "config": {"workload": args.workload, "rays_per_step": rays},
-        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": cores, "kind": kind,
+        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": cores, "cpu": host_cpu(), "kind": kind,
                          "sample": f"full workload ({rays} rays) per step, intersectVolume with "
                                    f"computeSurfaceProperties=true on {cores} host threads"},
         "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -421,7 +436,7 @@ def run_gpu(args, world, rank, local):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         dt, kind = cpu_trace(nodes, root, batches)
         cores = host_cores()
-        cpu = {"value": rays_per_step / dt / 1e6, "unit": "Mrays/s", "cores": cores, "kind": kind,
+        cpu = {"value": rays_per_step / dt / 1e6, "unit": "Mrays/s", "cores": cores, "cpu": host_cpu(), "kind": kind,
                "sample": f"one pass over the full workload ({rays_per_step} rays), {cores} host threads"}
 
     launches = args.steps * len(dev_batches)
@@ -503,7 +518,7 @@ def run_reference_batch(args, world, rank):
         "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (64 seeded volumes, generated rays)",
         "impl": "reference", "config": {"workload": "batch-64", "rays_per_step": rays, "volumes": len(jobs)},
-        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": cores, "kind": kind,
+        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": cores, "cpu": host_cpu(), "kind": kind,
                          "sample": f"all 64 volumes ({rays} rays) per step on {cores} host threads"},
         "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}), flush=True)
 
@@ -596,7 +611,7 @@ def run_gpu_batch(args, world, rank, local):
         for n, r, o, d in host_jobs:
             orc.intersect(n, orc.find_subdags(n, r), o, d)
         dt = time.perf_counter() - t0
-        cpu = {"value": rays_per_step / dt / 1e6, "unit": "Mrays/s", "cores": host_cores(), "kind": "port",
+        cpu = {"value": rays_per_step / dt / 1e6, "unit": "Mrays/s", "cores": host_cores(), "cpu": host_cpu(), "kind": "port",
                "sample": f"one pass over all 64 volumes ({rays_per_step} rays), {host_cores()} host threads"}
     batch_traffic = profiled_traffic("batch-64")  # DRAM bytes per ray, one launch (ncu)
     line = {

@@ -454,11 +454,20 @@ cbq_status cbq_intersect_host(const cbq_dag* cdag, const float* host_origin_tmax
         }
         dag->stage_capacity = n;
     }
-    if (!dag->pipe[0]) {
-        for (int k = 0; k < 4; k++)
-            if (cudaStreamCreateWithFlags(&dag->pipe[k], cudaStreamNonBlocking) != cudaSuccess) return CBQ_ERR_CUDA;
-        for (int k = 0; k < 2 * kHostChunksMax; k++)
-            if (cudaEventCreateWithFlags(&dag->pipe_ev[k], cudaEventDisableTiming) != cudaSuccess) return CBQ_ERR_CUDA;
+    if (!dag->pipe[0]) {  // created all together, or not at all
+        bool ok = true;
+        for (int k = 0; k < 4 && ok; k++)
+            ok = cudaStreamCreateWithFlags(&dag->pipe[k], cudaStreamNonBlocking) == cudaSuccess;
+        for (uint64_t k = 0; k < 2 * kHostChunksMax && ok; k++)
+            ok = cudaEventCreateWithFlags(&dag->pipe_ev[k], cudaEventDisableTiming) == cudaSuccess;
+        if (!ok) {
+            cudaGetLastError();
+            for (cudaStream_t& st : dag->pipe)
+                if (st) { cudaStreamDestroy(st); st = nullptr; }
+            for (cudaEvent_t& ev : dag->pipe_ev)
+                if (ev) { cudaEventDestroy(ev); ev = nullptr; }
+            return CBQ_ERR_CUDA;
+        }
     }
     char* p = (char*)dag->d_stage;
     float* d_o = (float*)p;

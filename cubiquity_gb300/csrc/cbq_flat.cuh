@@ -98,9 +98,10 @@ __device__ __forceinline__ void lane_begin(Lane& L, const Src& c, uint64_t i)
     L.roy = __fmul_rn(__fadd_rn(L.o.y, 0.5f), sy);
     L.roz = __fmul_rn(__fadd_rn(L.o.z, 0.5f), sz);
     const float rdx = fabsf(L.d.x), rdy = fabsf(L.d.y), rdz = fabsf(L.d.z);
-    L.ix = 1.0f / rdx;
-    L.iy = 1.0f / rdy;
-    L.iz = 1.0f / rdz;
+    // 1 / |dir|: the correctly rounded reciprocal, the same value as the IEEE division.
+    L.ix = __frcp_rn(rdx);
+    L.iy = __frcp_rn(rdy);
+    L.iz = __frcp_rn(rdz);
     L.oct = 0u;
     L.ddx = (-L.rox) / rdx;
     L.ddy = (-L.roy) / rdy;

@@ -290,9 +290,10 @@ __device__ __forceinline__ RayResult intersect_volume(const DagParams& dag, floa
     f.oy = __fmul_rn(__fadd_rn(o.y, 0.5f), sy);
     f.oz = __fmul_rn(__fadd_rn(o.z, 0.5f), sz);
     const float rdx = fabsf(d.x), rdy = fabsf(d.y), rdz = fabsf(d.z);
-    f.ix = 1.0f / rdx;
-    f.iy = 1.0f / rdy;
-    f.iz = 1.0f / rdz;
+    // 1 / |dir|: the correctly rounded reciprocal, the same value as the IEEE division.
+    f.ix = __frcp_rn(rdx);
+    f.iy = __frcp_rn(rdy);
+    f.iz = __frcp_rn(rdz);
 
     uint32_t oct = 0u;
     float dx = (-f.ox) / rdx, dy = (-f.oy) / rdy, dz = (-f.oz) / rdz;
