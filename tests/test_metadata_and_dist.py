@@ -97,3 +97,10 @@ def test_reference_arm_under_torchrun_two_ranks():
     import json
     j = json.loads(lines[0])
     assert j["impl"] == "reference" and j["value"] > 0 and j["n_gpus"] == 2
+    for key in ("metric", "unit", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling", "vs_baseline",
+                "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in j, key
+    assert j["config"]["workload"] == "spheres-256" and j["unit"] == "Mrays/s" and j["higher_is_better"] is True
+    cb = j["cpu_baseline"]
+    assert cb["value"] == j["value"] and cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["sample"]
+    assert j["e2e"] == {"value": j["value"], "unit": j["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
