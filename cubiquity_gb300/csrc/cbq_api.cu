@@ -14,7 +14,7 @@ using namespace cbq;
 
 namespace {
 
-constexpr int kFlatBlockDefault = 64;  // GB300 sweep, terrain-4096: 64 >= 128 > 256 threads
+constexpr int kFlatBlockDefault = 64;  // GB300, terrain-4096: 64, 128 and 256 threads within 1%
 constexpr uint32_t kRefillDefault = 8;
 
 bool use_flat(const cbq_dag* dag)
@@ -244,6 +244,13 @@ cbq_status cbq_dag_set_l2_persistence(const cbq_dag* dag, cbq_stream_t stream, f
     }
     if (cudaStreamSetAttribute((cudaStream_t)stream, cudaStreamAttributeAccessPolicyWindow, &attr) != cudaSuccess)
         return CBQ_ERR_CUDA;
+    if (fraction == 0.0f) {
+        // Give the set-aside back to normal caching, and demote lines already marked
+        // persisting (both settings belong to this process's context).
+        if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0) != cudaSuccess ||
+            cudaCtxResetPersistingL2Cache() != cudaSuccess)
+            return CBQ_ERR_CUDA;
+    }
     return CBQ_OK;
 }
 

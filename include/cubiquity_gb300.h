@@ -206,7 +206,12 @@ cbq_status cbq_autotune(cbq_dag* dag, const cbq_rays* rays, uint64_t n, const cb
                         cbq_launch_config* best, float* best_ms, cbq_stream_t stream);
 
 /* Sets a persisting-L2 access-policy window over the node store on `stream`
- * (fraction of the device's persisting-L2 limit to reserve, 0 disables). */
+ * (fraction of the device's persisting-L2 limit to reserve; 0 removes the window,
+ * releases the set-aside and demotes persisting lines).  The set-aside is a
+ * setting of the calling process's context.  Measured on GB300 it does not
+ * help: a DAG that fits in L2 already stays there, and the set-aside shrinks
+ * the cache left for the streamed rays and hits (terrain-4096: -2% primary,
+ * -5% bounce at fraction 1). */
 cbq_status cbq_dag_set_l2_persistence(const cbq_dag* dag, cbq_stream_t stream, float fraction);
 
 /* ------------------------------------------------------------ traversal */

@@ -78,3 +78,20 @@ def test_scratch_checks(scene):
     small = cbq.scratch_for(10)
     with pytest.raises(cbq.CbqError):
         cbq.intersect_auto(dag, o, d, small)
+
+
+def test_l2_persistence_window_keeps_results(scene):
+    """cbq_dag_set_l2_persistence marks the node store persisting in L2 for a
+    stream (a per-context setting): results are unchanged, and 0 clears it."""
+    dag, rays = scene
+    o, d = rays["bounce"]
+    want = cbq.intersect_volume(dag, o, d)
+    stream = torch.cuda.Stream()
+    dag.set_l2_persistence(1.0, stream=stream)
+    with torch.cuda.stream(stream):
+        got = cbq.intersect_volume(dag, o, d, stream=stream)
+    stream.synchronize()
+    _same(got, want)
+    dag.set_l2_persistence(0.0, stream=stream)
+    with pytest.raises(cbq.CbqError):
+        dag.set_l2_persistence(1.5)
