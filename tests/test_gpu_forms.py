@@ -95,3 +95,15 @@ def test_l2_persistence_window_keeps_results(scene):
     dag.set_l2_persistence(0.0, stream=stream)
     with pytest.raises(cbq.CbqError):
         dag.set_l2_persistence(1.5)
+
+
+def test_l2_probes():
+    """cbq_measure_l2: the streaming and random-sector L2 read rates used as the
+    traversal's L2 roofline are finite and ordered (random 32 B sectors move
+    fewer bytes per second than streaming reads)."""
+    torch.cuda.set_device(0)
+    stream_gbs, sectors_gsps = cbq.measure_l2(32 << 20, 5)
+    assert 1000.0 < stream_gbs < 100000.0
+    assert 1.0 < sectors_gsps and sectors_gsps * 32.0 < stream_gbs
+    with pytest.raises(cbq.CbqError):
+        cbq.measure_l2(32 << 20, 0)
