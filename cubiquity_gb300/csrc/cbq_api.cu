@@ -79,6 +79,36 @@ dev::HitsOut make_hits(const cbq_hits* h)
 
 bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 
+// The persistent form's work counter for launches on `stream` (one per stream,
+// allocated on first use), or nullptr where none can be had: the id query
+// fails, or the stream is being captured (no allocation inside a capture).
+uint64_t* stream_counter(const cbq_dag* cdag, cudaStream_t stream)
+{
+    cbq_dag* dag = const_cast<cbq_dag*>(cdag);
+    // Only the capture query is legal while a capture is under way: ask it first.
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &capture) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (capture != cudaStreamCaptureStatusNone) return nullptr;
+    unsigned long long id = 0;
+    if (cudaStreamGetId(stream, &id) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lk(dag->counter_lock);
+    auto it = dag->stream_counters.find(id);
+    if (it != dag->stream_counters.end()) return it->second;
+    uint64_t* p = nullptr;
+    if (cudaMalloc((void**)&p, 256) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    dag->stream_counters[id] = p;
+    return p;
+}
+
 cbq_status check_rays(const cbq_rays* rays)
 {
     if (!rays || !rays->origin_tmax || !rays->direction) return CBQ_ERR_INVALID_ARGUMENT;
@@ -200,7 +230,7 @@ cbq_status cbq_dag_destroy(cbq_dag* dag)
     if (!dag) return CBQ_ERR_INVALID_ARGUMENT;
     cudaFree(dag->d_nodes);
     if (dag->d_stage) cudaFree(dag->d_stage);
-    if (dag->d_counter) cudaFree(dag->d_counter);
+    for (auto& kv : dag->stream_counters) cudaFree(kv.second);
     for (cudaStream_t& st : dag->pipe)
         if (st) cudaStreamDestroy(st);
     for (cudaEvent_t& ev : dag->pipe_ev)
@@ -262,10 +292,14 @@ cbq_status cbq_intersect(const cbq_dag* dag, const cbq_rays* rays, uint64_t n, c
     if (n == 0) return CBQ_OK;  // an empty batch may carry NULL buffers
     cbq_status st = check_rays(rays);
     if (st != CBQ_OK) return st;
-    if (use_flat(dag))
+    if (use_flat(dag)) {
+        // The DAG's form: persistent (the default, with this stream's work counter) or plain.
+        uint64_t* counter = dag->cfg.form != CBQ_FORM_PLAIN ? stream_counter(dag, (cudaStream_t)stream) : nullptr;
+        const FlatLaunch fl = counter ? flat_launch(dag, true, counter, 0u) : flat_launch(dag, false, nullptr, 0u);
         return launch_flat(dag, make_dag_params(dag), make_query(query), make_hits(hits),
-                           (const float4*)rays->origin_tmax, (const float4*)rays->direction, n, nullptr,
-                           flat_launch(dag, false, nullptr, 0u), (cudaStream_t)stream);
+                           (const float4*)rays->origin_tmax, (const float4*)rays->direction, n, nullptr, fl,
+                           (cudaStream_t)stream);
+    }
     const uint64_t blocks = (n + kPlainBlock - 1) / kPlainBlock;
     if (blocks > 0x7fffffffull) return CBQ_ERR_INVALID_ARGUMENT;
     cbq_k_intersect_plain<<<(unsigned)blocks, kPlainBlock, 0, (cudaStream_t)stream>>>(

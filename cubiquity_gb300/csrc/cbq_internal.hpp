@@ -5,6 +5,7 @@
 #include "../../include/cubiquity_gb300.h"
 
 #include <cstdint>
+#include <map>
 #include <mutex>
 #include <vector>
 
@@ -67,7 +68,10 @@ struct cbq_dag {
     std::mutex staging_lock;
     void* d_stage = nullptr;
     uint64_t stage_capacity = 0;   // rays
-    uint64_t* d_counter = nullptr;
+    // Work counters of cbq_intersect's persistent form, one per stream id (ids are unique
+    // for the context's lifetime, so launches sharing a counter are ordered by their stream).
+    std::mutex counter_lock;
+    std::map<unsigned long long, uint64_t*> stream_counters;
     struct CUstream_st* pipe[4] = {};  // cudaStream_t (this header is also compiled without CUDA)
     struct CUevent_st* pipe_ev[2 * cbq::kHostChunksMax] = {};  // cudaEvent_t
 };

@@ -217,7 +217,11 @@ cbq_status cbq_dag_set_l2_persistence(const cbq_dag* dag, cbq_stream_t stream, f
 /* ------------------------------------------------------------ traversal */
 
 /* intersectVolume (raytracing.h:72-76 / raytracing.cpp:397-478) for n rays:
- * one launch, device rays in, device hits out.  The plain drop-in form. */
+ * one launch, device rays in, device hits out, stream-ordered.  It runs in the
+ * DAG's launch form: persistent by default, with a work counter the DAG keeps
+ * per stream (allocated on the first call on a stream, so launches sharing it
+ * are ordered by that stream), or one thread per ray for CBQ_FORM_PLAIN and
+ * while the stream is being captured into a graph. */
 cbq_status cbq_intersect(const cbq_dag* dag, const cbq_rays* rays, uint64_t n,
                          const cbq_query* query, const cbq_hits* hits, cbq_stream_t stream);
 

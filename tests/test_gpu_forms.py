@@ -107,3 +107,34 @@ def test_l2_probes():
     assert 1.0 < sectors_gsps and sectors_gsps * 32.0 < stream_gbs
     with pytest.raises(cbq.CbqError):
         cbq.measure_l2(32 << 20, 0)
+
+
+def test_drop_in_on_concurrent_streams_and_in_a_graph(scene):
+    """cbq_intersect's persistent form keeps one work counter per stream: launches
+    on several streams at once, and one captured into a CUDA graph (the plain
+    form there), give the plain form's bits."""
+    dag, rays = scene
+    o, d = rays["bounce"]
+    dag.set_launch_config(cbq.KERNEL_FLAT, 64, 0, 0, cbq.STACK_LOCAL, cbq.FORM_PLAIN)
+    parts = [(o[i::4].contiguous(), d[i::4].contiguous()) for i in range(4)]
+    want = [cbq.intersect_volume(dag, po, pd) for po, pd in parts]
+    dag.set_launch_config()
+    streams = [torch.cuda.Stream() for _ in parts]
+    outs = []
+    for _ in range(3):  # the same streams again: their counters are reused in stream order
+        outs = []
+        for s_, (po, pd) in zip(streams, parts):
+            with torch.cuda.stream(s_):
+                outs.append(cbq.intersect_volume(dag, po, pd, stream=s_))
+        torch.cuda.synchronize()
+        for got, w in zip(outs, want):
+            _same(got, w)
+    s_ = torch.cuda.Stream()
+    po, pd = parts[0]
+    out = cbq.alloc_hits(po.shape[0])
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s_):
+        cbq.intersect_volume(dag, po, pd, out=out, stream=s_)
+    g.replay()
+    torch.cuda.synchronize()
+    _same(out, want[0])
