@@ -11,10 +11,11 @@
 // whose ray is done pull new rays from a global counter (warp-aggregated).
 //
 // Floating-point operations are those of cbq_traverse.cuh / the reference, in
-// the same order (compile with -fmad=false).  Positions are carried both as
-// i32 (for the XOR/MSB pop logic) and as float copies updated by exact float
-// additions; the host only selects this form when every SubDAG's reflected
-// coordinates lie within +-2^24, where (float)(a + b) == (float)a + (float)b.
+// the same order (compile with -fmad=false).  Child positions are carried as
+// floats updated by exact float additions; the host only selects this form
+// when every SubDAG's reflected coordinates lie within +-2^24, where
+// (float)(a + b) == (float)a + (float)b, so the i32 positions the pop's
+// XOR/MSB logic needs are recovered exactly by conversion when a pop happens.
 #pragma once
 
 #include "../../include/cubiquity_gb300.h"
@@ -33,7 +34,7 @@ struct Lane {
     uint32_t sign, oct;
     // ESVO walk state
     uint32_t node, cid, written;
-    int32_t cx, cy, cz, cns;
+    int32_t cns;
     float fx, fy, fz, fcns;
     int h, start_h;
     float last_exit;
@@ -198,9 +199,6 @@ __device__ __forceinline__ void lane_enter(Lane& L, const Src& c)
     L.cns = (int32_t)(ns >> 1);
     L.fcns = (float)L.cns;
     L.cid = first_child_f(L, entry, fpx + L.fcns, fpy + L.fcns, fpz + L.fcns);
-    L.cx = px + ((L.cid & 1u) ? L.cns : 0);
-    L.cy = py + ((L.cid & 2u) ? L.cns : 0);
-    L.cz = pz + ((L.cid & 4u) ? L.cns : 0);
     L.fx = fpx + ((L.cid & 1u) ? L.fcns : 0.0f);
     L.fy = fpy + ((L.cid & 2u) ? L.fcns : 0.0f);
     L.fz = fpz + ((L.cid & 4u) ? L.fcns : 0.0f);
@@ -235,9 +233,9 @@ __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
             L.cns >>= 1;
             L.fcns = (float)L.cns;
             L.cid = first_child_f(L, tce, L.fx + L.fcns, L.fy + L.fcns, L.fz + L.fcns);
-            if (L.cid & 1u) { L.cx += L.cns; L.fx += L.fcns; }
-            if (L.cid & 2u) { L.cy += L.cns; L.fy += L.fcns; }
-            if (L.cid & 4u) { L.cz += L.cns; L.fz += L.fcns; }
+            if (L.cid & 1u) L.fx += L.fcns;
+            if (L.cid & 2u) L.fy += L.fcns;
+            if (L.cid & 4u) L.fz += L.fcns;
         } else {
             uint32_t material = 0u;
             float nx = 0.0f, ny = 0.0f, nz = 0.0f;
@@ -262,12 +260,16 @@ __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
         return;
     }
     L.cid ^= flips;
-    const int32_t ox = L.cx, oy = L.cy, oz = L.cz;
-    if (flips & 1u) { L.cx += L.cns; L.fx += L.fcns; }
-    if (flips & 2u) { L.cy += L.cns; L.fy += L.fcns; }
-    if (flips & 4u) { L.cz += L.cns; L.fz += L.fcns; }
+    if (flips & 1u) L.fx += L.fcns;
+    if (flips & 2u) L.fy += L.fcns;
+    if (flips & 4u) L.fz += L.fcns;
     if ((L.cid & flips) != flips) {
-        const uint32_t diff = (uint32_t)(ox ^ L.cx) | (uint32_t)(oy ^ L.cy) | (uint32_t)(oz ^ L.cz);
+        // Integer positions from the exact float ones (|p| < 2^24); on a flipped axis the
+        // position before the advance was p - childSize.
+        const int32_t cx = __float2int_rz(L.fx), cy = __float2int_rz(L.fy), cz = __float2int_rz(L.fz);
+        const uint32_t diff = ((flips & 1u) ? (uint32_t)(cx ^ (cx - L.cns)) : 0u) |
+                              ((flips & 2u) ? (uint32_t)(cy ^ (cy - L.cns)) : 0u) |
+                              ((flips & 4u) ? (uint32_t)(cz ^ (cz - L.cns)) : 0u);
         const int msb = 31 - __clz(diff);
         const int h = msb + 1;
         if (h > L.start_h) {  // left the sub-DAG: on to the next octant
@@ -278,15 +280,12 @@ __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
         L.node = (L.written & (1u << h)) ? stack.get(h) : 0u;
         L.cns = (int32_t)(1u << msb);
         L.fcns = (float)L.cns;
-        L.cid = (((uint32_t)L.cx >> msb) & 1u) | ((((uint32_t)L.cy >> msb) & 1u) << 1) |
-                ((((uint32_t)L.cz >> msb) & 1u) << 2);
+        L.cid = (((uint32_t)cx >> msb) & 1u) | ((((uint32_t)cy >> msb) & 1u) << 1) |
+                ((((uint32_t)cz >> msb) & 1u) << 2);
         const uint32_t keep = 0u - (uint32_t)L.cns;
-        L.cx = (int32_t)((uint32_t)L.cx & keep);
-        L.cy = (int32_t)((uint32_t)L.cy & keep);
-        L.cz = (int32_t)((uint32_t)L.cz & keep);
-        L.fx = (float)L.cx;
-        L.fy = (float)L.cy;
-        L.fz = (float)L.cz;
+        L.fx = (float)(int32_t)((uint32_t)cx & keep);
+        L.fy = (float)(int32_t)((uint32_t)cy & keep);
+        L.fz = (float)(int32_t)((uint32_t)cz & keep);
         L.last_exit = 0.0f;
     }
 }
