@@ -775,11 +775,15 @@ def run_gpu_serve(args, world, rank, local):
     clocks.start()
     # Three 4 s runs at half load; the line reports the run with the median p99
     # (host jitter from other work on the machine moves single-run tails).
+    import gc
+    gc.collect()
+    gc.disable()  # no collector pauses in the Python load generator while it runs
     halves = [open_loop(0.5 * peak_rps, 4.0, 5000 + 40000 * k) for k in range(3)]
     clk = clocks.stop()
     half = dict(sorted(halves, key=lambda r: r["p99_ms"])[1])
     half["p99_ms_runs"] = [r["p99_ms"] for r in halves]
     sweep = [open_loop(f * peak_rps, 2.0, 9000 + int(f * 1000)) for f in (0.25, 0.75)]
+    gc.enable()
     server.close()
     line = {
         "metric": "p99 latency at 50% of peak load", "value": half["p99_ms"], "unit": "ms", "n_gpus": world,
