@@ -35,6 +35,7 @@ namespace {
 using Clock = std::chrono::steady_clock;
 
 constexpr uint64_t kAlign = 256;
+constexpr size_t kInlineMaxInflight = 2;  // submit launches by itself below this many launches in flight
 constexpr uint64_t kBytesPerRay = 16 + 16 + 12 + 12 + 12 + 4 + 4 + 1 + 1;  // rays in, all hit fields out
 
 uint64_t align_up(uint64_t v) { return (v + kAlign - 1) & ~(kAlign - 1); }
@@ -47,6 +48,7 @@ struct Request {
     uint64_t bytes = 0;      // pool bytes (0 for a direct request)
     uint64_t offset = 0;
     bool direct = false;     // served in place: the kernel reads and writes the caller's host buffers
+    bool out_async = true;   // every hit buffer is page-locked (a copy into it does not block the host)
     const float* d_o = nullptr;
     const float* d_d = nullptr;
     cbq_hits d_hits{};
@@ -66,6 +68,26 @@ const void* device_alias(const void* p)
     if (a.type == cudaMemoryTypeHost && a.devicePointer) return a.devicePointer;
     if (a.type == cudaMemoryTypeManaged) return p;
     return nullptr;
+}
+
+// True when a device-to-host copy into `p` is asynchronous: page-locked or
+// managed host memory (into pageable memory the copy blocks the calling thread).
+bool copy_into_is_async(const void* p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type != cudaMemoryTypeUnregistered;
+}
+
+bool hits_copy_async(const cbq_hits& h)
+{
+    const void* fields[] = {h.hit, h.distance, h.material, h.position, h.normal, h.voxel, h.status};
+    for (const void* f : fields)
+        if (f && !copy_into_is_async(f)) return false;
+    return true;
 }
 
 // Resolves every buffer of a request to a device alias; false if any needs staging.
@@ -168,6 +190,7 @@ struct cbq_server {
     std::condition_variable cv_sched, cv_complete, cv_done;
     bool stopping = false;
     bool scheduler_done = false;
+    int inline_pending = 0;   // launches being enqueued by submitting threads
     uint64_t next_ticket = 1;
     uint64_t completions = 0;  // generation count, bumped per finished launch
     std::thread scheduler, completer;
@@ -181,7 +204,32 @@ struct cbq_server {
     void run_scheduler();
     void run_completer();
     cbq_status enqueue(Slot& s, const std::vector<Request*>& group);
+    cbq_status copy_hits_back(const Request* rq, cudaStream_t stream) const;
+    // Enqueues `group` on slot `si` (already taken) with `lk` released, then hands the
+    // slot to the completion thread.  Called with `lk` held; returns with it held.
+    void launch_group(int si, std::vector<Request*>& group, std::unique_lock<std::mutex>& lk);
 };
+
+void cbq_server::launch_group(int si, std::vector<Request*>& group, std::unique_lock<std::mutex>& lk)
+{
+    lk.unlock();
+    int prev = device;
+    cudaGetDevice(&prev);
+    if (prev != device) cudaSetDevice(device);  // a submitting thread may have another device current
+    const cbq_status st = enqueue(slots[si], group);
+    if (st != CBQ_OK) {
+        cudaGetLastError();
+        for (Request* rq : group) rq->status = st;
+        cudaEventRecord(slots[si].done, slots[si].stream);
+    }
+    if (prev != device) cudaSetDevice(prev);
+    lk.lock();
+    slots[si].reqs = group;
+    inflight.push_back(si);
+    launches++;
+    launched_requests += group.size();
+    cv_complete.notify_one();
+}
 
 cbq_status cbq_server::enqueue(Slot& s, const std::vector<Request*>& group)
 {
@@ -263,22 +311,30 @@ cbq_status cbq_server::enqueue(Slot& s, const std::vector<Request*>& group)
                                             device, s.stream);
         if (st != CBQ_OK) return st;
     }
-    // Results back to the host.
+    // Results back to page-locked host buffers; pageable ones are copied by the completion
+    // thread once the launch is done, so that this thread never waits for the device.
     for (Request* rq : group) {
-        if (rq->direct) continue;
-        const uint64_t n = rq->r.ray_count;
-        char* h = d_pool + rq->offset + n * 32;
-        const cbq_hits& hh = rq->r.host_hits;
-        struct Copy { void* dst; size_t bytes; };
-        const Copy copies[] = {{hh.position, n * 12}, {hh.normal, n * 12}, {hh.voxel, n * 12},
-                               {hh.distance, n * 4}, {hh.material, n * 4}, {hh.hit, n}, {hh.status, n}};
-        for (const Copy& c : copies) {
-            if (c.dst && cudaMemcpyAsync(c.dst, h, c.bytes, cudaMemcpyDeviceToHost, s.stream) != cudaSuccess)
-                return CBQ_ERR_CUDA;
-            h += align_up(c.bytes);
-        }
+        if (rq->direct || !rq->out_async) continue;
+        const cbq_status st = copy_hits_back(rq, s.stream);
+        if (st != CBQ_OK) return st;
     }
     return cudaEventRecord(s.done, s.stream) == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
+}
+
+cbq_status cbq_server::copy_hits_back(const Request* rq, cudaStream_t stream) const
+{
+    const uint64_t n = rq->r.ray_count;
+    char* h = d_pool + rq->offset + n * 32;
+    const cbq_hits& hh = rq->r.host_hits;
+    struct Copy { void* dst; size_t bytes; };
+    const Copy copies[] = {{hh.position, n * 12}, {hh.normal, n * 12}, {hh.voxel, n * 12},
+                           {hh.distance, n * 4}, {hh.material, n * 4}, {hh.hit, n}, {hh.status, n}};
+    for (const Copy& c : copies) {
+        if (c.dst && cudaMemcpyAsync(c.dst, h, c.bytes, cudaMemcpyDeviceToHost, stream) != cudaSuccess)
+            return CBQ_ERR_CUDA;
+        h += align_up(c.bytes);
+    }
+    return CBQ_OK;
 }
 
 void cbq_server::run_scheduler()
@@ -308,19 +364,7 @@ void cbq_server::run_scheduler()
         }
         const int si = free_slots.front();
         free_slots.pop_front();
-        lk.unlock();
-        const cbq_status st = enqueue(slots[si], group);
-        if (st != CBQ_OK) {
-            cudaGetLastError();
-            for (Request* rq : group) rq->status = st;
-            cudaEventRecord(slots[si].done, slots[si].stream);
-        }
-        lk.lock();
-        slots[si].reqs = group;
-        inflight.push_back(si);
-        launches++;
-        launched_requests += group.size();
-        cv_complete.notify_one();
+        launch_group(si, group, lk);
     }
     scheduler_done = true;
     cv_complete.notify_all();
@@ -331,11 +375,24 @@ void cbq_server::run_completer()
     cudaSetDevice(device);
     std::unique_lock<std::mutex> lk(mu);
     for (;;) {
-        cv_complete.wait(lk, [&] { return !inflight.empty() || scheduler_done; });
+        cv_complete.wait(lk, [&] { return !inflight.empty() || (scheduler_done && inline_pending == 0); });
         if (inflight.empty()) break;  // scheduler finished and everything completed
         const int si = inflight.front();
         lk.unlock();
         const bool ok = cudaEventSynchronize(slots[si].done) == cudaSuccess;
+        if (ok) {  // hits for pageable buffers: copied now that the launch is done
+            bool any = false;
+            for (Request* rq : slots[si].reqs) {
+                if (rq->direct || rq->out_async || rq->status != CBQ_OK) continue;
+                any = true;
+                if (copy_hits_back(rq, slots[si].stream) != CBQ_OK) rq->status = CBQ_ERR_CUDA;
+            }
+            if (any && cudaStreamSynchronize(slots[si].stream) != cudaSuccess) {
+                cudaGetLastError();
+                for (Request* rq : slots[si].reqs)
+                    if (!rq->direct && !rq->out_async && rq->status == CBQ_OK) rq->status = CBQ_ERR_CUDA;
+            }
+        }
         const Clock::time_point now = Clock::now();
         lk.lock();
         inflight.pop_front();
@@ -424,11 +481,12 @@ cbq_status cbq_server_submit(cbq_server* s, const cbq_request* r, uint64_t* tick
     rq->r = *r;
     rq->direct = r->ray_count > 0 && (s->cfg.flags & CBQ_SERVER_IN_PLACE) && resolve_direct(*rq);
     rq->bytes = rq->direct ? 0 : request_bytes(r->ray_count);
+    rq->out_async = rq->direct || hits_copy_async(r->host_hits);
     if (rq->bytes > s->cfg.device_memory_budget) {
         delete rq;
         return CBQ_ERR_CAPACITY;
     }
-    std::lock_guard<std::mutex> lk(s->mu);
+    std::unique_lock<std::mutex> lk(s->mu);
     if (s->stopping) { delete rq; return CBQ_ERR_SHUTDOWN; }
     rq->ticket = s->next_ticket++;
     *ticket = rq->ticket;
@@ -442,6 +500,22 @@ cbq_status cbq_server_submit(cbq_server* s, const cbq_request* r, uint64_t* tick
         return CBQ_OK;
     }
     s->live[rq->ticket] = 1;
+    // A lightly loaded device (nothing queued, under two launches in flight), a slot and
+    // memory free: launch from this thread, one thread hand-off fewer than through the
+    // scheduler (arrival order is kept).  Under load, requests queue and leave in groups.
+    uint64_t off = 0;
+    if (s->queue.empty() && s->inflight.size() + s->inline_pending < kInlineMaxInflight &&
+        !s->free_slots.empty() && (rq->bytes == 0 || s->pool.alloc(rq->bytes, &off))) {
+        rq->offset = off;
+        const int si = s->free_slots.front();
+        s->free_slots.pop_front();
+        s->inline_pending++;
+        std::vector<Request*> group{rq};
+        s->launch_group(si, group, lk);
+        s->inline_pending--;
+        s->cv_complete.notify_one();
+        return CBQ_OK;
+    }
     s->queue.push_back(rq);
     s->cv_sched.notify_one();
     return CBQ_OK;
