@@ -16,8 +16,10 @@
  *     position / normal / voxel hold three values per ray (x, y, z interleaved).
  *   - Launching calls are stream-ordered and asynchronous on `stream`
  *     (a cudaStream_t; NULL = legacy default stream).
- *   - A cbq_dag is immutable once created and may be used from several host
- *     threads and streams at once.
+ *   - A cbq_dag's node store is immutable once created; the handle may be used
+ *     from several host threads and streams at once.  Its launch configuration
+ *     (cbq_dag_set_launch_config, cbq_autotune) is the one mutable part: change
+ *     it while no other thread launches on the handle.
  */
 #ifndef CUBIQUITY_GB300_H
 #define CUBIQUITY_GB300_H
