@@ -228,8 +228,10 @@ cbq_status cbq_intersect(const cbq_dag* dag, const cbq_rays* rays, uint64_t n,
                          const cbq_query* query, const cbq_hits* hits, cbq_stream_t stream);
 
 /* As cbq_intersect, with HOST rays and HOST hits: copies in, traverses, copies
- * out, and waits for completion.  Allocates and caches device staging buffers
- * per dag (serialised by a per-dag lock). */
+ * out, and waits for completion.  Calls of 2^19 rays or more are split into up
+ * to 8 chunks whose copies overlap the traversal of their neighbours (own
+ * streams; page-locked host buffers copy fastest).  Allocates and caches device
+ * staging buffers per dag; calls on one dag are serialised by a per-dag lock. */
 cbq_status cbq_intersect_host(const cbq_dag* dag, const float* host_origin_tmax,
                               const float* host_direction, uint64_t n, const cbq_query* query,
                               const cbq_hits* host_hits);
