@@ -342,7 +342,7 @@ def run_gpu(args, world, rank, local):
         if tuned:
             c = tuned[label]
             dag.set_launch_config(c["kernel"], c["block"], c["chunk"], c["refill_min"], c["stack"], c["form"],
-                                  c.get("steps", 1))
+                                  c.get("steps", 1), c.get("registers", 0))
             cbq.intersect_auto(dag, to, td, scratch, out=out, stream=stream)
         elif args.persistent:
             cbq.intersect_volume_persistent(dag, to, td, counter, chunk=args.chunk, out=out, stream=stream)

@@ -76,11 +76,11 @@ class LaunchConfig(ctypes.Structure):
     """cbq_launch_config."""
     _fields_ = [("kernel", ctypes.c_int32), ("block", ctypes.c_int32), ("chunk", ctypes.c_uint32),
                 ("refill_min", ctypes.c_uint32), ("stack", ctypes.c_int32), ("form", ctypes.c_int32),
-                ("steps", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("steps", ctypes.c_int32), ("registers", ctypes.c_int32)]
 
     def as_dict(self):
         return {"kernel": self.kernel, "block": self.block, "chunk": self.chunk, "refill_min": self.refill_min,
-                "stack": self.stack, "form": self.form, "steps": self.steps}
+                "stack": self.stack, "form": self.form, "steps": self.steps, "registers": self.registers}
 
 
 class _DagInfo(ctypes.Structure):
@@ -389,8 +389,8 @@ class Dag:
 
     def set_launch_config(self, kernel: int = KERNEL_AUTO, block: int = 0, chunk: int = 0,
                           refill_min: int = 0, stack: int = STACK_LOCAL, form: int = FORM_PERSISTENT,
-                          steps: int = 8) -> None:
-        cfg = LaunchConfig(kernel, block, chunk, refill_min, stack, form, steps, 0)
+                          steps: int = 8, registers: int = 0) -> None:
+        cfg = LaunchConfig(kernel, block, chunk, refill_min, stack, form, steps, registers)
         _check(_lib.cbq_dag_set_launch_config(self.handle, ctypes.byref(cfg)), "cbq_dag_set_launch_config")
 
     def launch_config(self) -> dict:

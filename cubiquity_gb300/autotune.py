@@ -68,8 +68,9 @@ def tune(dag: cbq.Dag, origin_tmax, direction, scratch, out: dict, compute_surfa
     if key in cache:
         cfg = dict(cache[key]["config"])
         cfg.setdefault("steps", 1)
+        cfg.setdefault("registers", 0)
         dag.set_launch_config(cfg["kernel"], cfg["block"], cfg["chunk"], cfg["refill_min"], cfg["stack"], cfg["form"],
-                              cfg["steps"])
+                              cfg["steps"], cfg["registers"])
         return dict(cfg, cached=True, key=key)
     cfg, ms = cbq.autotune_launch(dag, origin_tmax, direction, scratch, out, compute_surface_properties,
                                   max_footprint, use_tmax, repetitions, stream)

@@ -33,6 +33,7 @@ FlatLaunch flat_launch(const cbq_dag* dag, bool persistent, uint64_t* counter, u
     fl.refill_min = refill ? refill : (dag->cfg.refill_min ? dag->cfg.refill_min : kRefillDefault);
     fl.local_stack = dag->cfg.stack == CBQ_STACK_LOCAL;
     fl.steps = dag->cfg.steps > 0 ? (uint32_t)dag->cfg.steps : 1u;
+    fl.registers56 = dag->cfg.registers == 56;
     return fl;
 }
 
@@ -317,6 +318,7 @@ cbq_status cbq_dag_set_launch_config(cbq_dag* dag, const cbq_launch_config* cfg)
     if (cfg->stack != CBQ_STACK_SHARED && cfg->stack != CBQ_STACK_LOCAL) return CBQ_ERR_INVALID_ARGUMENT;
     if (cfg->form < CBQ_FORM_PLAIN || cfg->form > CBQ_FORM_SORTED) return CBQ_ERR_INVALID_ARGUMENT;
     if (cfg->steps < 0 || cfg->steps > 16) return CBQ_ERR_INVALID_ARGUMENT;
+    if (cfg->registers != 0 && cfg->registers != 56) return CBQ_ERR_INVALID_ARGUMENT;
     if (cfg->kernel == CBQ_KERNEL_NESTED && dag->layout == CBQ_DAG_LAYOUT_COMPACT) return CBQ_ERR_INVALID_ARGUMENT;
     dag->cfg = *cfg;
     return CBQ_OK;
@@ -373,15 +375,19 @@ cbq_status cbq_autotune(cbq_dag* dag, const cbq_rays* rays, uint64_t n, const cb
         for (int blk : blocks) {
             for (uint32_t rf : refills) {
                 if (form == CBQ_FORM_PLAIN && rf != refills[0]) continue;  // refill unused
-                for (int stk_steps = 0; stk_steps < 8; stk_steps++) {
-                    const int stk = stacks[stk_steps & 1];
+                // stack x steps, plus the 56-register kernel for the persistent local-stack form
+                for (int v = 0; v < 12; v++) {
+                    const int stk = v < 8 ? stacks[v & 1] : CBQ_STACK_LOCAL;
+                    const int regs = v < 8 ? 0 : 56;
+                    if (regs && form == CBQ_FORM_PLAIN) continue;
                     cbq_launch_config c = saved;
                     c.kernel = dag->flat_ok ? CBQ_KERNEL_FLAT : CBQ_KERNEL_NESTED;
                     c.block = dag->flat_ok ? blk : 0;
                     c.refill_min = rf;
                     c.stack = stk;
                     c.form = form;
-                    c.steps = step_counts[stk_steps >> 1];
+                    c.steps = v < 8 ? step_counts[v >> 1] : step_counts[v - 8];
+                    c.registers = regs;
                     dag->cfg = c;
                     st = cbq_intersect_auto(dag, rays, n, query, hits, scratch, scratch_bytes, stream);  // warm-up
                     if (st != CBQ_OK) break;
@@ -405,9 +411,10 @@ cbq_status cbq_autotune(cbq_dag* dag, const cbq_rays* rays, uint64_t n, const cb
     cudaEventDestroy(e1);
     dag->cfg = st == CBQ_OK ? winner : saved;
     if (st == CBQ_OK)
-        cbq::log(CBQ_LOG_INFO, "autotune over %llu rays: form %d, block %d, refill %u, stack %s, steps %d: %.3f ms",
+        cbq::log(CBQ_LOG_INFO,
+                 "autotune over %llu rays: form %d, block %d, refill %u, stack %s, steps %d, registers %d: %.3f ms",
                  (unsigned long long)n, winner.form, winner.block, winner.refill_min,
-                 winner.stack == CBQ_STACK_LOCAL ? "local" : "shared", winner.steps, win_ms);
+                 winner.stack == CBQ_STACK_LOCAL ? "local" : "shared", winner.steps, winner.registers, win_ms);
     if (best) *best = dag->cfg;
     if (best_ms) *best_ms = st == CBQ_OK ? win_ms : 0.0f;
     return st;

@@ -21,9 +21,8 @@ constexpr unsigned kFull = 0xffffffffu;
 // SORTED: ray g of the launch is ray perm[g] of the input (octant order).
 // Ctx: FlatCtxT of the node store layout.
 template <bool PERSISTENT, bool SHARED, bool SORTED, typename Ctx>
-__global__ void __launch_bounds__(256) cbq_k_flat(Ctx c, uint64_t n, unsigned long long* __restrict__ counter,
-                                                  uint32_t refill_min, const uint32_t* __restrict__ perm,
-                                                  uint32_t steps)
+__device__ __forceinline__ void flat_body(const Ctx& c, uint64_t n, unsigned long long* __restrict__ counter,
+                                          uint32_t refill_min, const uint32_t* __restrict__ perm, uint32_t steps)
 {
     extern __shared__ uint32_t smem_stack[];
     SharedStack sstack;
@@ -68,6 +67,26 @@ __global__ void __launch_bounds__(256) cbq_k_flat(Ctx c, uint64_t n, unsigned lo
         else
             lane_walk_steps(L, c, lstack, steps);
     }
+}
+
+template <bool PERSISTENT, bool SHARED, bool SORTED, typename Ctx>
+__global__ void __launch_bounds__(256) cbq_k_flat(Ctx c, uint64_t n, unsigned long long* __restrict__ counter,
+                                                  uint32_t refill_min, const uint32_t* __restrict__ perm,
+                                                  uint32_t steps)
+{
+    flat_body<PERSISTENT, SHARED, SORTED>(c, n, counter, refill_min, perm, steps);
+}
+
+// The persistent local-stack form held to 56 registers per thread: 36 resident
+// warps per SM instead of 32 with blocks of 64 or 128 threads.  Measured on
+// GB300 it is the faster choice for incoherent (bounce) rays, so the tuner
+// tries it (launch config `registers` = 56).
+template <bool SORTED, typename Ctx>
+__global__ void __maxnreg__(56) cbq_k_flat_r56(Ctx c, uint64_t n, unsigned long long* __restrict__ counter,
+                                               uint32_t refill_min, const uint32_t* __restrict__ perm,
+                                               uint32_t steps)
+{
+    flat_body<true, false, SORTED>(c, n, counter, refill_min, perm, steps);
 }
 
 // Octant of a ray: its direction sign bits (raytracing.cpp:416-417).
@@ -155,13 +174,16 @@ cbq_status launch_variant(const Ctx& c, uint64_t n, const FlatLaunch& fl, int ro
     } else {
         int sms = 0, per_sm = 0;
         if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return CBQ_ERR_CUDA;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::cbq_k_flat<true, S, O, Ctx>, fl.block, smem) !=
-            cudaSuccess)
+        auto kernel = dev::cbq_k_flat<true, S, O, Ctx>;
+        if constexpr (!S) {
+            if (fl.registers56) kernel = dev::cbq_k_flat_r56<O, Ctx>;
+        }
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, fl.block, smem) != cudaSuccess)
             return CBQ_ERR_CUDA;
         per_sm = std::max(per_sm, 1);
         if (cudaMemsetAsync(fl.counter, 0, sizeof(uint64_t), stream) != cudaSuccess) return CBQ_ERR_CUDA;
-        dev::cbq_k_flat<true, S, O, Ctx><<<sms * per_sm, fl.block, smem, stream>>>(
-            c, n, (unsigned long long*)fl.counter, fl.refill_min, fl.perm, fl.steps ? fl.steps : 1u);
+        kernel<<<sms * per_sm, fl.block, smem, stream>>>(c, n, (unsigned long long*)fl.counter, fl.refill_min,
+                                                          fl.perm, fl.steps ? fl.steps : 1u);
     }
     return cudaGetLastError() == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
 }

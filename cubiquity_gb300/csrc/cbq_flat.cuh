@@ -332,6 +332,7 @@ struct FlatLaunch {
     bool local_stack = false;        // descent stack in local memory instead of shared
     const uint32_t* perm = nullptr;  // octant-sorted order (from launch_octant_sort), or null
     uint32_t steps = 1;              // ESVO steps per outer loop iteration
+    bool registers56 = false;        // persistent local-stack form held to 56 registers
 };
 
 }  // namespace cbq

@@ -183,7 +183,8 @@ typedef struct cbq_launch_config {
     int32_t stack;            /* CBQ_STACK_* (flat kernel) */
     int32_t form;             /* CBQ_FORM_*, used by cbq_intersect_auto */
     int32_t steps;            /* flat kernel: ESVO steps per loop iteration (1..16), 0 = 1 */
-    int32_t reserved;
+    int32_t registers;        /* 0, or 56: the persistent local-stack kernel held to 56
+                                 registers per thread (more resident warps) */
 } cbq_launch_config;
 
 cbq_status cbq_dag_set_launch_config(cbq_dag* dag, const cbq_launch_config* cfg);
@@ -200,8 +201,8 @@ cbq_status cbq_intersect_auto(const cbq_dag* dag, const cbq_rays* rays, uint64_t
                               const cbq_hits* hits, void* scratch, uint64_t scratch_bytes, cbq_stream_t stream);
 
 /* Autotuner: times every form x block {64,128,256} x refill {4,8,16} x stack
- * {shared, local} x steps {2,4,8,16} on these rays (synchronous; `repetitions`
- * launches each),
+ * {shared, local} x steps {2,4,8,16}, and the 56-register persistent
+ * local-stack kernel, on these rays (synchronous; `repetitions` launches each),
  * stores the fastest in the DAG's launch config and returns it with its time. */
 cbq_status cbq_autotune(cbq_dag* dag, const cbq_rays* rays, uint64_t n, const cbq_query* query,
                         const cbq_hits* hits, void* scratch, uint64_t scratch_bytes, int32_t repetitions,

@@ -138,3 +138,21 @@ def test_drop_in_on_concurrent_streams_and_in_a_graph(scene):
     g.replay()
     torch.cuda.synchronize()
     _same(out, want[0])
+
+
+@pytest.mark.parametrize("form", [cbq.FORM_PERSISTENT, cbq.FORM_SORTED])
+@pytest.mark.parametrize("block,steps", [(64, 8), (128, 16), (256, 4)])
+def test_register_capped_kernel_equals_the_drop_in(scene, form, block, steps):
+    """The persistent local-stack kernel held to 56 registers (launch config
+    registers = 56) gives the same bits; other register values are refused."""
+    dag, rays = scene
+    scratch = cbq.scratch_for(max(o.shape[0] for o, _ in rays.values()))
+    for label, (o, d) in rays.items():
+        dag.set_launch_config(cbq.KERNEL_FLAT, 64, 0, 0, cbq.STACK_LOCAL, cbq.FORM_PLAIN)
+        want = cbq.intersect_volume(dag, o, d)
+        dag.set_launch_config(cbq.KERNEL_FLAT, block, 0, 8, cbq.STACK_LOCAL, form, steps, registers=56)
+        assert dag.launch_config()["registers"] == 56
+        _same(cbq.intersect_auto(dag, o, d, scratch), want)
+    with pytest.raises(cbq.CbqError):
+        dag.set_launch_config(registers=48)
+    dag.set_launch_config()
