@@ -40,9 +40,9 @@ constexpr unsigned kFullMask = 0xffffffffu;
 // the faster choices for the single-volume kernel on GB300.  Every job of one
 // launch has the node store layout COMPACT.
 template <bool COMPACT>
-__global__ void __launch_bounds__(256) cbq_k_flat_batch(const JobDesc* __restrict__ jobs, uint32_t njobs,
-                                                        uint64_t total, unsigned long long* __restrict__ counter,
-                                                        uint32_t refill_min, uint32_t steps)
+__device__ __forceinline__ void batch_body(const JobDesc* __restrict__ jobs, uint32_t njobs, uint64_t total,
+                                           unsigned long long* __restrict__ counter, uint32_t refill_min,
+                                           uint32_t steps)
 {
     extern __shared__ uint64_t prefix[];  // njobs + 1 entries
     LocalStack stack;
@@ -94,6 +94,24 @@ __global__ void __launch_bounds__(256) cbq_k_flat_batch(const JobDesc* __restric
     }
 }
 
+template <bool COMPACT>
+__global__ void __launch_bounds__(256) cbq_k_flat_batch(const JobDesc* __restrict__ jobs, uint32_t njobs,
+                                                        uint64_t total, unsigned long long* __restrict__ counter,
+                                                        uint32_t refill_min, uint32_t steps)
+{
+    batch_body<COMPACT>(jobs, njobs, total, counter, refill_min, steps);
+}
+
+// The same held to 56 registers per thread (more resident warps); a batch
+// autotuner choice like the single-volume kernel's.
+template <bool COMPACT>
+__global__ void __maxnreg__(56) cbq_k_flat_batch_r56(const JobDesc* __restrict__ jobs, uint32_t njobs,
+                                                     uint64_t total, unsigned long long* __restrict__ counter,
+                                                     uint32_t refill_min, uint32_t steps)
+{
+    batch_body<COMPACT>(jobs, njobs, total, counter, refill_min, steps);
+}
+
 }  // namespace dev
 
 void fill_job_volume(dev::JobDesc& d, const cbq_dag* dag)
@@ -114,9 +132,10 @@ namespace {
 
 template <bool COMPACT>
 cbq_status launch_batch_layout(const dev::JobDesc* d_jobs, uint32_t njobs, uint64_t total, uint64_t* counter,
-                               int block, uint32_t refill, uint32_t steps, int device, cudaStream_t s)
+                               int block, uint32_t refill, uint32_t steps, bool registers56, int device,
+                               cudaStream_t s)
 {
-    const auto kernel = dev::cbq_k_flat_batch<COMPACT>;
+    const auto kernel = registers56 ? dev::cbq_k_flat_batch_r56<COMPACT> : dev::cbq_k_flat_batch<COMPACT>;
     if (cudaMemsetAsync(counter, 0, sizeof(uint64_t), s) != cudaSuccess) return CBQ_ERR_CUDA;
     const size_t smem = (size_t)(njobs + 1) * 8;  // the prefix offsets
     if (smem > 227u * 1024u) return CBQ_ERR_CAPACITY;
@@ -135,12 +154,15 @@ cbq_status launch_batch_layout(const dev::JobDesc* d_jobs, uint32_t njobs, uint6
 }  // namespace
 
 cbq_status launch_batch_kernel(const dev::JobDesc* d_jobs, uint32_t njobs, uint64_t total, uint64_t* counter,
-                               int block, uint32_t refill, uint32_t steps, bool compact, int device, cudaStream_t s)
+                               int block, uint32_t refill, uint32_t steps, bool compact, int device, cudaStream_t s,
+                               bool registers56)
 {
     if (total == 0 || njobs == 0) return CBQ_OK;
     if (steps == 0) steps = 1;
-    return compact ? launch_batch_layout<true>(d_jobs, njobs, total, counter, block, refill, steps, device, s)
-                   : launch_batch_layout<false>(d_jobs, njobs, total, counter, block, refill, steps, device, s);
+    return compact ? launch_batch_layout<true>(d_jobs, njobs, total, counter, block, refill, steps, registers56,
+                                               device, s)
+                   : launch_batch_layout<false>(d_jobs, njobs, total, counter, block, refill, steps, registers56,
+                                                device, s);
 }
 
 }  // namespace cbq
@@ -162,6 +184,7 @@ struct cbq_batch {
     uint64_t total = 0;
     uint64_t total_ref = 0;
     uint32_t steps = kBatchStepsDefault;
+    bool registers56 = false;
     uint64_t* d_counter = nullptr;
     cbq_query query{1, CBQ_MAX_FOOTPRINT_DISABLED, 0u, 0u};
     int block = kBatchBlockDefault;
@@ -179,10 +202,10 @@ cbq_status enqueue_batch(cbq_batch* b, cudaStream_t s)
         if (st != CBQ_OK) return st;
     }
     cbq_status st = launch_batch_kernel(b->d_jobs, b->njobs_ref, b->total_ref, b->d_counter, b->block, b->refill,
-                                        b->steps, false, b->device, s);
+                                        b->steps, false, b->device, s, b->registers56);
     if (st != CBQ_OK) return st;
     return launch_batch_kernel(b->d_jobs + b->njobs_ref, b->njobs - b->njobs_ref, b->total - b->total_ref,
-                               b->d_counter + 8, b->block, b->refill, b->steps, true, b->device, s);
+                               b->d_counter + 8, b->block, b->refill, b->steps, true, b->device, s, b->registers56);
 }
 
 void drop_graph(cbq_batch* b)
@@ -328,13 +351,15 @@ cbq_status cbq_batch_autotune(cbq_batch* b, cbq_stream_t stream, int32_t repetit
     float best = 1e30f;
     int best_block = b->block;
     uint32_t best_refill = b->refill, best_steps = b->steps;
+    bool best_r56 = b->registers56;
     cbq_status st = CBQ_OK;
-    for (int k = 0; k < 3 * 4 * 3 && st == CBQ_OK; k++) {
-        const int blk = blocks[k / 12];
-        const uint32_t rf = refills[(k / 3) % 4];
+    for (int k = 0; k < 3 * 4 * 3 * 2 && st == CBQ_OK; k++) {
+        const int blk = blocks[k / 24];
+        const uint32_t rf = refills[(k / 6) % 4];
         b->block = blk;
         b->refill = rf;
-        b->steps = step_counts[k % 3];
+        b->steps = step_counts[(k / 2) % 3];
+        b->registers56 = (k & 1) != 0;
         st = enqueue_batch(b, (cudaStream_t)stream);  // warm-up
         if (st != CBQ_OK) break;
         cudaEventRecord(e0, (cudaStream_t)stream);
@@ -343,17 +368,25 @@ cbq_status cbq_batch_autotune(cbq_batch* b, cbq_stream_t stream, int32_t repetit
         if (st != CBQ_OK || cudaEventSynchronize(e1) != cudaSuccess) { st = CBQ_ERR_CUDA; break; }
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
-        if (ms < best) { best = ms; best_block = blk; best_refill = rf; best_steps = b->steps; }
+        if (ms < best) {
+            best = ms;
+            best_block = blk;
+            best_refill = rf;
+            best_steps = b->steps;
+            best_r56 = b->registers56;
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     b->block = best_block;
     b->refill = best_refill;
     b->steps = best_steps;
+    b->registers56 = best_r56;
     drop_graph(b);
     if (st == CBQ_OK)
-        cbq::log(CBQ_LOG_INFO, "batch autotune: block %d, refill %u, %u steps per iteration: %.3f ms per launch",
-                 best_block, best_refill, best_steps, best / (float)repetitions);
+        cbq::log(CBQ_LOG_INFO,
+                 "batch autotune: block %d, refill %u, %u steps per iteration, %d registers: %.3f ms per launch",
+                 best_block, best_refill, best_steps, best_r56 ? 56 : 64, best / (float)repetitions);
     return st;
 }
 

@@ -35,7 +35,7 @@ void fill_job_volume(dev::JobDesc& d, const cbq_dag* dag);
 // `stream` first.
 cbq_status launch_batch_kernel(const dev::JobDesc* d_jobs, uint32_t njobs, uint64_t total, uint64_t* counter,
                                int block, uint32_t refill, uint32_t steps, bool compact, int device,
-                               cudaStream_t stream);
+                               cudaStream_t stream, bool registers56 = false);
 
 constexpr uint32_t kBatchStepsDefault = 8;
 
