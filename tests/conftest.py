@@ -10,6 +10,22 @@ if str(ROOT) not in sys.path:
 GOLDEN = Path(__file__).resolve().parent / "golden"
 
 
+def _ensure_library():
+    """Builds libcbq.so before the test modules import the package, when a
+    session starts without it (the package itself refuses to import without
+    the library: there is no CPU fallback)."""
+    if (ROOT / "cubiquity_gb300" / "libcbq.so").exists():
+        return
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_cbq_build", ROOT / "cubiquity_gb300" / "_build.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    mod.build()
+
+
+_ensure_library()
+
+
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs the sm_103a kernels)")
     config.addinivalue_line("markers", "reference: needs the reference checkout (oracle/_ref)")
