@@ -244,19 +244,20 @@ cbq_status launch_flat(const cbq_dag* dag, const dev::DagParams& dp, const dev::
     if (fl.perm && n >= 0xffffffffull) return CBQ_ERR_INVALID_ARGUMENT;
     const int rows = std::max(1, (int)dag->max_height);
     const int dv = dag->device;
-    if (dag->layout == CBQ_DAG_LAYOUT_COMPACT) {
-        if (fetch_out) {  // load counting: one shape
-            using Ctx = dev::FlatCtxT<true, true>;
-            FlatLaunch one = fl;
-            one.persistent = false;
-            one.local_stack = true;
-            one.perm = nullptr;
-            return launch_variant<false, false, false>(make_ctx<Ctx>(dp, q, out, orig, dir, fetch_out), n, one, rows,
-                                                       stream, dv);
-        }
-        return launch_ctx(make_ctx<dev::FlatCtxT<true>>(dp, q, out, orig, dir, nullptr), n, fl, rows, stream, dv);
+    if (fetch_out) {  // fetch / load counting: its own instantiation, one shape
+        FlatLaunch one = fl;
+        one.persistent = false;
+        one.local_stack = true;
+        one.perm = nullptr;
+        if (dag->layout == CBQ_DAG_LAYOUT_COMPACT)
+            return launch_variant<false, false, false>(
+                make_ctx<dev::FlatCtxT<true, true>>(dp, q, out, orig, dir, fetch_out), n, one, rows, stream, dv);
+        return launch_variant<false, false, false>(
+            make_ctx<dev::FlatCtxT<false, true>>(dp, q, out, orig, dir, fetch_out), n, one, rows, stream, dv);
     }
-    return launch_ctx(make_ctx<dev::FlatCtxT<false>>(dp, q, out, orig, dir, fetch_out), n, fl, rows, stream, dv);
+    if (dag->layout == CBQ_DAG_LAYOUT_COMPACT)
+        return launch_ctx(make_ctx<dev::FlatCtxT<true>>(dp, q, out, orig, dir, nullptr), n, fl, rows, stream, dv);
+    return launch_ctx(make_ctx<dev::FlatCtxT<false>>(dp, q, out, orig, dir, nullptr), n, fl, rows, stream, dv);
 }
 
 }  // namespace cbq
