@@ -183,8 +183,9 @@ typedef struct cbq_launch_config {
     int32_t stack;            /* CBQ_STACK_* (flat kernel) */
     int32_t form;             /* CBQ_FORM_*, used by cbq_intersect_auto */
     int32_t steps;            /* flat kernel: ESVO steps per loop iteration (1..16), 0 = 1 */
-    int32_t registers;        /* 0, or 56: the persistent local-stack kernel held to 56
-                                 registers per thread (more resident warps) */
+    int32_t registers;        /* 0, or 56 (the default): the persistent local-stack
+                                 kernel held to 56 registers per thread (more
+                                 resident warps); other forms ignore it */
 } cbq_launch_config;
 
 cbq_status cbq_dag_set_launch_config(cbq_dag* dag, const cbq_launch_config* cfg);
