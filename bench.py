@@ -418,10 +418,14 @@ def run_gpu(args, world, rank, local):
                 "material": torch.empty(n, dtype=torch.int32).pin_memory(),
                 "position": torch.empty((n, 3), dtype=torch.float32).pin_memory(),
                 "normal": torch.empty((n, 3), dtype=torch.float32).pin_memory()}
-        host.append((po.numpy(), pd.numpy(), {k: v.numpy() for k, v in outs.items()}))
+        host.append((label, po.numpy(), pd.numpy(), {k: v.numpy() for k, v in outs.items()}))
 
     def e2e_step():
-        for po, pd, outs in host:
+        for label, po, pd, outs in host:
+            if tuned:  # the launch shape tuned for this batch, as a caller who tuned would set it
+                c = tuned[label]
+                dag.set_launch_config(c["kernel"], c["block"], c["chunk"], c["refill_min"], c["stack"], c["form"],
+                                      c.get("steps", 1), c.get("registers", 0))
             cbq.intersect_volume_host(dag, po, pd, out=outs)
 
     e2e_step()

@@ -301,8 +301,9 @@ __device__ __forceinline__ void lane_walk_steps(Lane& L, const Src& c, Stack& st
 {
     if (L.mode != kLaneWalk) return;
     const uint32_t budget = kMaxFetches - L.fetches;  // > 0: a walking lane is below the cap
-    const uint32_t n = steps < budget ? steps : budget;
-    for (uint32_t k = 0; k < n && L.mode == kLaneWalk; k++) lane_walk(L, c, stack);
+    // Every step makes one fetch, so the fetch count doubles as the step counter.
+    const uint32_t end = L.fetches + (steps < budget ? steps : budget);
+    while (L.fetches < end && L.mode == kLaneWalk) lane_walk(L, c, stack);
     if (L.mode == kLaneWalk && L.fetches >= kMaxFetches) {
         L.status = kRayIterLimit;
         lane_finish(L, c, false, 0.0f, 0u, 0.0f, 0.0f, 0.0f);
