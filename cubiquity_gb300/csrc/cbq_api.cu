@@ -80,6 +80,62 @@ dev::HitsOut make_hits(const cbq_hits* h)
 
 bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 
+// One chunk of a cbq_intersect_host call.  The call's rays are cut into blocks of
+// `block` consecutive rays dealt round-robin to the chunks (block b to chunk
+// b % chunks), so that every chunk samples the whole batch: a camera batch whose
+// first rows are sky and whose middle rows are terrain gives chunks of equal work,
+// and the copies and traversals of consecutive chunks stay balanced.  On the
+// device a chunk's rays and hits are contiguous, from ray `start`; on the host its
+// full blocks are the rows of a pitched array, and the batch's last, partial block
+// (if this chunk has it) is copied on its own.
+struct HostChunk {
+    uint64_t block = 1;    // rays per block
+    uint64_t start = 0;    // first ray of the chunk in the device staging
+    uint64_t rows = 0;     // full blocks: host blocks k, k + chunks, ...
+    uint64_t tail = 0;     // rays of the batch's partial last block, if this chunk has it
+    uint64_t tail_at = 0;  // host index of that block's first ray
+    uint64_t rays() const { return rows * block + tail; }
+};
+
+HostChunk host_chunk(uint64_t n, uint64_t chunks, uint64_t block, uint64_t k, uint64_t start)
+{
+    const uint64_t full = n / block, rem = n % block;
+    HostChunk c;
+    c.block = block;
+    c.start = start;
+    c.rows = full > k ? (full - k + chunks - 1) / chunks : 0;
+    if (rem != 0 && full % chunks == k) {
+        c.tail = rem;
+        c.tail_at = full * block;
+    }
+    return c;
+}
+
+// Copies `width` bytes per ray of chunk k between the host array (every ray of the
+// call) and the device array (the chunk's rays from c.start).
+bool copy_chunk(void* host, void* dev, size_t width, const HostChunk& c, uint64_t k, uint64_t chunks,
+                cudaMemcpyKind kind, cudaStream_t s)
+{
+    char* h = (char*)host;
+    char* d = (char*)dev + c.start * width;
+    const size_t row = c.block * width;
+    const bool in = kind == cudaMemcpyHostToDevice;
+    if (c.rows != 0) {
+        char* hr = h + k * row;
+        const cudaError_t e = in ? cudaMemcpy2DAsync(d, row, hr, chunks * row, row, c.rows, kind, s)
+                                 : cudaMemcpy2DAsync(hr, chunks * row, d, row, row, c.rows, kind, s);
+        if (e != cudaSuccess) return false;
+    }
+    if (c.tail != 0) {
+        char* ht = h + c.tail_at * width;
+        char* dt = d + c.rows * row;
+        const cudaError_t e = in ? cudaMemcpyAsync(dt, ht, c.tail * width, kind, s)
+                                 : cudaMemcpyAsync(ht, dt, c.tail * width, kind, s);
+        if (e != cudaSuccess) return false;
+    }
+    return true;
+}
+
 // The persistent form's work counter for launches on `stream` (one per stream,
 // allocated on first use), or nullptr where none can be had: the id query
 // fails, or the stream is being captured (no allocation inside a capture).
@@ -537,18 +593,20 @@ cbq_status cbq_intersect_host(const cbq_dag* cdag, const float* host_origin_tmax
     // copied in and chunk k - 1 copied out.  Consecutive chunks are traversed on alternating
     // streams, so the next chunk's blocks fill the SMs while the previous launch drains (a
     // persistent launch ends with a tail of few busy warps).  Events order each chunk's copy in,
-    // traversal and copy out.
+    // traversal and copy out.  Chunks interleave blocks of the batch (HostChunk).
     const uint64_t chunks = std::min<uint64_t>(kHostChunksMax, std::max<uint64_t>(1, n / kHostChunkMin));
-    const uint64_t per_chunk = (n + chunks - 1) / chunks;
     cudaStream_t s_in = dag->pipe[0], s_out = dag->pipe[1];
-    for (uint64_t k = 0; k * per_chunk < n; k++) {
+    const uint64_t block = std::max<uint64_t>(kHostBlockMin, n / (chunks * kHostBlocksPerChunk));
+    uint64_t start = 0;
+    for (uint64_t k = 0; k < chunks; k++) {
+        const HostChunk hc = host_chunk(n, chunks, block, k, start);
+        const uint64_t a = start, m = hc.rays();
+        start += m;
+        if (m == 0) continue;
         cudaStream_t s_run = dag->pipe[2 + (k & 1)];
-        const uint64_t a = k * per_chunk, m = std::min(per_chunk, n - a);
         cudaEvent_t copied = dag->pipe_ev[2 * k], traversed = dag->pipe_ev[2 * k + 1];
-        if (cudaMemcpyAsync(d_o + 4 * a, host_origin_tmax + 4 * a, m * 16, cudaMemcpyHostToDevice, s_in) !=
-                cudaSuccess ||
-            cudaMemcpyAsync(d_d + 4 * a, host_direction + 4 * a, m * 16, cudaMemcpyHostToDevice, s_in) !=
-                cudaSuccess ||
+        if (!copy_chunk((void*)host_origin_tmax, d_o, 16, hc, k, chunks, cudaMemcpyHostToDevice, s_in) ||
+            !copy_chunk((void*)host_direction, d_d, 16, hc, k, chunks, cudaMemcpyHostToDevice, s_in) ||
             cudaEventRecord(copied, s_in) != cudaSuccess || cudaStreamWaitEvent(s_run, copied, 0) != cudaSuccess)
             return CBQ_ERR_CUDA;
         cbq_hits launch;
@@ -566,18 +624,18 @@ cbq_status cbq_intersect_host(const cbq_dag* cdag, const float* host_origin_tmax
         if (st != CBQ_OK) return st;
         if (cudaEventRecord(traversed, s_run) != cudaSuccess || cudaStreamWaitEvent(s_out, traversed, 0) != cudaSuccess)
             return CBQ_ERR_CUDA;
-        struct Copy { void* dst; const void* src; size_t bytes; };
-        const Copy copies[] = {
-            {host_hits->hit ? host_hits->hit + a : nullptr, launch.hit, m},
-            {host_hits->distance ? host_hits->distance + a : nullptr, launch.distance, m * 4},
-            {host_hits->material ? host_hits->material + a : nullptr, launch.material, m * 4},
-            {host_hits->position ? host_hits->position + 3 * a : nullptr, launch.position, m * 12},
-            {host_hits->normal ? host_hits->normal + 3 * a : nullptr, launch.normal, m * 12},
-            {host_hits->voxel ? host_hits->voxel + 3 * a : nullptr, launch.voxel, m * 12},
-            {host_hits->status ? host_hits->status + a : nullptr, launch.status, m}};
+        struct Copy {
+            void* host;
+            void* dev;
+            size_t width;
+        };
+        const Copy copies[] = {{host_hits->hit, dh.hit, 1},           {host_hits->distance, dh.distance, 4},
+                               {host_hits->material, dh.material, 4}, {host_hits->position, dh.position, 12},
+                               {host_hits->normal, dh.normal, 12},    {host_hits->voxel, dh.voxel, 12},
+                               {host_hits->status, dh.status, 1}};
         for (const Copy& c : copies) {
-            if (!c.dst) continue;
-            if (cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToHost, s_out) != cudaSuccess)
+            if (!c.host) continue;
+            if (!copy_chunk(c.host, c.dev, c.width, hc, k, chunks, cudaMemcpyDeviceToHost, s_out))
                 return CBQ_ERR_CUDA;
         }
     }

@@ -44,6 +44,10 @@ cbq_status build_compact(const uint32_t* nodes, uint64_t node_count, const cbq_s
 // least kHostChunkMin rays.
 constexpr uint64_t kHostChunksMax = 8;
 constexpr uint64_t kHostChunkMin = 1ull << 18;
+// ... each made of about kHostBlocksPerChunk blocks of consecutive rays (at least
+// kHostBlockMin) dealt round-robin.
+constexpr uint64_t kHostBlocksPerChunk = 4;
+constexpr uint64_t kHostBlockMin = 4096;
 
 }  // namespace cbq
 

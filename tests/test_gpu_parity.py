@@ -172,10 +172,11 @@ def test_host_api_equals_device_api(terrain):
     _assert_same(c, {k: v[:1000] for k, v in a.items()}, FIELDS, what="host api reuse")
 
 
-@pytest.mark.parametrize("n", [(1 << 18) - 1, 3 * (1 << 18) + 17, 2_500_003])
+@pytest.mark.parametrize("n", [4095, (1 << 18) - 1, 3 * (1 << 18) + 17, 8 << 18, (8 << 18) + 4095, 2_500_003])
 def test_host_api_chunks(terrain, n):
     """Large host calls are split into chunks whose copies overlap the traversal
-    (one chunk per 2^18 rays, at most 8): every chunk size and boundary gives
+    (one chunk per 2^18 rays, at most 8), each chunk taking every k-th block of
+    4096 rays: every chunk count, block boundary and partial last block gives
     the device path's bits, with all or some hit fields requested, from
     pageable or page-locked buffers."""
     nodes, root, dag, o, d = terrain
