@@ -596,6 +596,12 @@ cbq_status cbq_intersect_host(const cbq_dag* cdag, const float* host_origin_tmax
     // traversal and copy out.  Chunks interleave blocks of the batch (HostChunk).
     const uint64_t chunks = std::min<uint64_t>(kHostChunksMax, std::max<uint64_t>(1, n / kHostChunkMin));
     cudaStream_t s_in = dag->pipe[0], s_out = dag->pipe[1];
+    // Every queued copy and launch ends before the call returns (the staging buffers are reused).
+    auto drain = [&](cbq_status st) {
+        bool ok = true;
+        for (cudaStream_t s : dag->pipe) ok = cudaStreamSynchronize(s) == cudaSuccess && ok;
+        return ok ? st : CBQ_ERR_CUDA;
+    };
     const uint64_t block = std::max<uint64_t>(kHostBlockMin, n / (chunks * kHostBlocksPerChunk));
     uint64_t start = 0;
     for (uint64_t k = 0; k < chunks; k++) {
@@ -608,7 +614,7 @@ cbq_status cbq_intersect_host(const cbq_dag* cdag, const float* host_origin_tmax
         if (!copy_chunk((void*)host_origin_tmax, d_o, 16, hc, k, chunks, cudaMemcpyHostToDevice, s_in) ||
             !copy_chunk((void*)host_direction, d_d, 16, hc, k, chunks, cudaMemcpyHostToDevice, s_in) ||
             cudaEventRecord(copied, s_in) != cudaSuccess || cudaStreamWaitEvent(s_run, copied, 0) != cudaSuccess)
-            return CBQ_ERR_CUDA;
+            return drain(CBQ_ERR_CUDA);
         cbq_hits launch;
         launch.hit = host_hits->hit ? dh.hit + a : nullptr;
         launch.distance = host_hits->distance ? dh.distance + a : nullptr;
@@ -621,9 +627,9 @@ cbq_status cbq_intersect_host(const cbq_dag* cdag, const float* host_origin_tmax
         // Persistent form; each chunk's counter is private to this call (staging lock held).
         cbq_status st = cbq_intersect_persistent(dag, &rays, m, query, &launch, d_counters + 8 * k, 0u,
                                                  (cbq_stream_t)s_run);
-        if (st != CBQ_OK) return st;
+        if (st != CBQ_OK) return drain(st);
         if (cudaEventRecord(traversed, s_run) != cudaSuccess || cudaStreamWaitEvent(s_out, traversed, 0) != cudaSuccess)
-            return CBQ_ERR_CUDA;
+            return drain(CBQ_ERR_CUDA);
         struct Copy {
             void* host;
             void* dev;
@@ -636,12 +642,10 @@ cbq_status cbq_intersect_host(const cbq_dag* cdag, const float* host_origin_tmax
         for (const Copy& c : copies) {
             if (!c.host) continue;
             if (!copy_chunk(c.host, c.dev, c.width, hc, k, chunks, cudaMemcpyDeviceToHost, s_out))
-                return CBQ_ERR_CUDA;
+                return drain(CBQ_ERR_CUDA);
         }
     }
-    bool ok = true;
-    for (cudaStream_t st : dag->pipe) ok = cudaStreamSynchronize(st) == cudaSuccess && ok;
-    return ok ? CBQ_OK : CBQ_ERR_CUDA;
+    return drain(CBQ_OK);
 }
 
 }  // extern "C"

@@ -232,8 +232,11 @@ cbq_status cbq_intersect(const cbq_dag* dag, const cbq_rays* rays, uint64_t n,
 /* As cbq_intersect, with HOST rays and HOST hits: copies in, traverses, copies
  * out, and waits for completion.  Calls of 2^19 rays or more are split into up
  * to 8 chunks whose copies overlap the traversal of their neighbours (own
- * streams; page-locked host buffers copy fastest).  Allocates and caches device
- * staging buffers per dag; calls on one dag are serialised by a per-dag lock. */
+ * streams; page-locked host buffers copy fastest); each chunk takes every k-th
+ * of about 4k blocks of consecutive rays, so chunks carry even work.  Allocates
+ * and caches device staging buffers per dag; calls on one dag are serialised by
+ * a per-dag lock.  On an error every copy and launch it queued has ended before
+ * it returns. */
 cbq_status cbq_intersect_host(const cbq_dag* dag, const float* host_origin_tmax,
                               const float* host_direction, uint64_t n, const cbq_query* query,
                               const cbq_hits* host_hits);
