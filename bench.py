@@ -528,7 +528,7 @@ def run_reference_batch(args, world, rank):
 
 
 def run_gpu_batch(args, world, rank, local):
-    """configs[2]: many volumes of uneven size in one persistent, graph-captured,
+    """batch-64: many volumes of uneven size in one persistent, graph-captured,
     autotuned launch, against the plain kernel launched once per volume."""
     import torch
     import cubiquity_gb300 as cbq
@@ -659,7 +659,7 @@ def run_gpu_batch(args, world, rank, local):
 
 
 def run_gpu_serve(args, world, rank, local):
-    """configs[3]: 8 resident terrain DAGs (edges 1024-4096); requests of 1k-256k
+    """serve-8: 8 resident terrain DAGs (edges 1024-4096); requests of 1k-256k
     rays (log-uniform), 70% tmax-bounded collision rays and 30% view rays.
     Finds the peak request rate closed-loop, then drives an open-loop Poisson
     stream at half of it and reports p50/p99 latency (submit -> hits in host
@@ -814,7 +814,7 @@ def run_gpu_serve(args, world, rank, local):
 
 
 def run_gpu_city(args, world, rank, local):
-    """configs[4]: the wavefront pathtracer on the seeded 8192^3 city,
+    """city-8192: the wavefront pathtracer on the seeded 8192^3 city,
     1920x1080, 16 samples per pixel, 4 bounces, LOD footprint 0.0035.  One
     step = one frame.  A 1-sample frame is also traced with every traversal
     wave checked against the oracle on the host."""
