@@ -190,6 +190,34 @@ def test_host_api_chunks(terrain, n):
     _assert_same(got, want, ("hit", "voxel", "status"), what=f"host chunks {n}, pinned, some fields")
 
 
+def test_host_api_from_several_threads(terrain):
+    """Host calls from four threads on one DAG handle (serialised by its staging
+    lock, each on the handle's own streams) give every thread its own bits."""
+    import threading
+    nodes, root, dag, o, d = terrain
+    n = 600_000
+    parts = [(_spread(o, 4 * n)[k::4], _spread(d, 4 * n)[k::4]) for k in range(4)]
+    want = [_host(cbq.intersect_volume(dag, _dev(po), _dev(pd))) for po, pd in parts]
+    got = [None] * 4
+    errors = []
+
+    def worker(k):
+        try:
+            for _ in range(3):
+                got[k] = cbq.intersect_volume_host(dag, *parts[k])
+        except Exception as e:  # noqa: BLE001  (reported below)
+            errors.append(e)
+
+    th = [threading.Thread(target=worker, args=(k,)) for k in range(4)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert not errors, errors
+    for k in range(4):
+        _assert_same(got[k], want[k], FIELDS + ("status",), what=f"thread {k}")
+
+
 def test_fetch_counts_match_oracle(terrain, orc):
     nodes, root, dag, o, d = terrain
     n = 200_000
