@@ -1,7 +1,8 @@
 // Wavefront pathtracer on top of the traversal (cbq_pathtrace).
 //
 // Restates the reference's CPU pathtracer (pathtracing_demo.cpp:81-190:
-// traceSingleRayRecurse / gatherLighting) as GPU waves.  Per sample pass:
+// traceSingleRayRecurse / gatherLighting) as GPU waves.  Per pass (as many
+// samples per pixel as fit in kPtRaysPerPass paths, traced together):
 //   camera rays -> [extension traversal -> shade -> shadow traversal -> add]
 //   repeated for depth 0..bounces
 // Shading follows the reference: a hit multiplies the path throughput by the
@@ -28,13 +29,17 @@
 namespace {
 
 struct PathState {
-    uint32_t pixel;
+    uint32_t pixel, sample;
     float tr, tg, tb;  // throughput
 };
 
+// Paths traced together in one pass: the samples of a pass share each wave's
+// launches (fewer, larger launches; one host round trip per depth and pass).
+constexpr uint64_t kPtRaysPerPass = 1ull << 24;
+
 struct Frame {
     int width, height;
-    uint32_t sample;
+    uint32_t sample, samples;  // the pass's first sample and its sample count
     uint64_t seed;
     float ex, ey, ez;              // eye
     float fx, fy, fz;              // forward
@@ -90,13 +95,15 @@ __device__ __forceinline__ float3 normalize3(float3 v)
     return l > 0.0f ? make_float3(v.x / l, v.y / l, v.z / l) : make_float3(0.0f, 0.0f, 1.0f);
 }
 
+// Path i of a pass: pixel i % npix of sample f.sample + i / npix.
 __global__ void cbq_k_pt_camera(Frame f, float4* __restrict__ o, float4* __restrict__ d, PathState* __restrict__ st)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t n = (uint32_t)f.width * (uint32_t)f.height;
-    if (i >= n) return;
-    const uint32_t px = i % (uint32_t)f.width, py = i / (uint32_t)f.width;
-    uint64_t h = rng_key(f.seed, i, f.sample, 0, 0);
+    const uint32_t npix = (uint32_t)f.width * (uint32_t)f.height;
+    if (i >= npix * f.samples) return;
+    const uint32_t pixel = i % npix, sample = f.sample + i / npix;
+    const uint32_t px = pixel % (uint32_t)f.width, py = pixel / (uint32_t)f.width;
+    uint64_t h = rng_key(f.seed, pixel, sample, 0, 0);
     const float jx = u01(h), jy = u01(h);
     const float sx = (((px + jx) / f.width) * 2.0f - 1.0f) * f.aspect * f.tan_half;
     const float sy = (1.0f - ((py + jy) / f.height) * 2.0f) * f.tan_half;
@@ -104,7 +111,7 @@ __global__ void cbq_k_pt_camera(Frame f, float4* __restrict__ o, float4* __restr
                                               f.fz + f.rz * sx + f.uz * sy));
     o[i] = make_float4(f.ex, f.ey, f.ez, __int_as_float(0x7f800000));
     d[i] = make_float4(dir.x, dir.y, dir.z, 0.0f);
-    st[i] = PathState{i, 1.0f, 1.0f, 1.0f};
+    st[i] = PathState{pixel, sample, 1.0f, 1.0f, 1.0f};
 }
 
 __device__ __forceinline__ void add_pixel(float* image, uint32_t pixel, float r, float g, float b)
@@ -127,8 +134,7 @@ __device__ __forceinline__ uint32_t append_slot(uint32_t* counter, bool want)
     return base + __popc(mask & ((1u << lane) - 1u));
 }
 
-__global__ void cbq_k_pt_shade(const Shading* __restrict__ sh, uint32_t n, uint32_t depth, uint32_t sample,
-                               uint64_t seed, int last, const PathState* __restrict__ st,
+__global__ void cbq_k_pt_shade(const Shading* __restrict__ sh, uint32_t n, uint32_t depth, uint64_t seed, int last, const PathState* __restrict__ st,
                                const uint8_t* __restrict__ hit, const uint32_t* __restrict__ material,
                                const float* __restrict__ position, const float* __restrict__ normal,
                                float* __restrict__ image, float4* __restrict__ so, float4* __restrict__ sd,
@@ -138,7 +144,7 @@ __global__ void cbq_k_pt_shade(const Shading* __restrict__ sh, uint32_t n, uint3
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = i < n;
-    PathState p{0u, 0.0f, 0.0f, 0.0f};
+    PathState p{0u, 0u, 0.0f, 0.0f, 0.0f};
     bool h = false;
     if (live) {
         p = st[i];
@@ -156,7 +162,7 @@ __global__ void cbq_k_pt_shade(const Shading* __restrict__ sh, uint32_t n, uint3
         tr = p.tr * sh->albedo[m][0];
         tg = p.tg * sh->albedo[m][1];
         tb = p.tb * sh->albedo[m][2];
-        key = rng_key(seed, p.pixel, sample, depth + 1, 0);
+        key = rng_key(seed, p.pixel, p.sample, depth + 1, 0);
     }
     // Two shadow rays per hit: sun and sky.
     const uint32_t s0 = append_slot(shadow_count, h);
@@ -185,7 +191,7 @@ __global__ void cbq_k_pt_shade(const Shading* __restrict__ sh, uint32_t n, uint3
         no[b] = make_float4(pos.x + nrm.x * 0.01f, pos.y + nrm.y * 0.01f, pos.z + nrm.z * 0.01f,
                             __int_as_float(0x7f800000));
         nd[b] = make_float4(dir.x, dir.y, dir.z, 0.0f);
-        nst[b] = PathState{p.pixel, tr, tg, tb};
+        nst[b] = PathState{p.pixel, p.sample, tr, tg, tb};
     }
 }
 
@@ -259,8 +265,10 @@ extern "C" cbq_status cbq_pathtrace(const cbq_dag* dag, const cbq_pt_config* cfg
             host_sh.emission[m][a] = cfg->materials[m].emission[a];
         }
 
-    // Buffers for one sample pass: two extension sets (ping-pong) and the shadow set.
-    const size_t ext = npix, sha = 2 * npix;
+    // Buffers for one pass: two extension sets (ping-pong) and the shadow set.
+    const uint64_t per_pass = std::max<uint64_t>(
+        1, std::min<uint64_t>((uint64_t)cfg->samples_per_pixel, kPtRaysPerPass / npix));
+    const size_t ext = npix * per_pass, sha = 2 * ext;
     const size_t per_ext = 2 * 16 + sizeof(PathState) + 1 + 4 + 12 + 12;
     const size_t bytes = 2 * (ext * per_ext) + sha * (16 * 3 + 1) + sizeof(Shading) + 32 * 256;  // + carve padding
     char* base = nullptr;
@@ -309,11 +317,13 @@ extern "C" cbq_status cbq_pathtrace(const cbq_dag* dag, const cbq_pt_config* cfg
 
     const cbq_query qext{1, cfg->max_footprint, 0u, 0u};
     const cbq_query qsh{0, cfg->max_footprint, 0u, 0u};
-    for (int sample = 0; sample < cfg->samples_per_pixel && st == CBQ_OK; sample++) {
+    for (int sample = 0; sample < cfg->samples_per_pixel && st == CBQ_OK; sample += (int)per_pass) {
+        const uint32_t samples = (uint32_t)std::min<uint64_t>(per_pass, (uint64_t)(cfg->samples_per_pixel - sample));
         Frame fr;
         fr.width = cfg->width;
         fr.height = cfg->height;
         fr.sample = (uint32_t)sample;
+        fr.samples = samples;
         fr.seed = cfg->seed;
         fr.ex = (float)cfg->eye[0];
         fr.ey = (float)cfg->eye[1];
@@ -323,9 +333,10 @@ extern "C" cbq_status cbq_pathtrace(const cbq_dag* dag, const cbq_pt_config* cfg
         fr.ux = (float)u[0]; fr.uy = (float)u[1]; fr.uz = (float)u[2];
         fr.tan_half = (float)cfg->tan_half_fov;
         fr.aspect = (float)cfg->width / (float)cfg->height;
-        cbq_k_pt_camera<<<(unsigned)((npix + 255) / 256), 256, 0, s>>>(fr, e[0].o, e[0].d, e[0].st);
+        const uint64_t paths = npix * samples;
+        cbq_k_pt_camera<<<(unsigned)((paths + 255) / 256), 256, 0, s>>>(fr, e[0].o, e[0].d, e[0].st);
         launches++;
-        uint32_t n = (uint32_t)npix;
+        uint32_t n = (uint32_t)paths;
         int cur = 0;
         for (int depth = 0; depth <= cfg->bounces && n > 0 && st == CBQ_OK; depth++) {
             Ext& E = e[cur];
@@ -342,7 +353,7 @@ extern "C" cbq_status cbq_pathtrace(const cbq_dag* dag, const cbq_pt_config* cfg
             }
             if (cudaMemsetAsync(counters, 0, 8 * sizeof(uint32_t), s) != cudaSuccess) { fail(CBQ_ERR_CUDA); break; }
             const int last = depth == cfg->bounces;
-            cbq_k_pt_shade<<<(n + 255) / 256, 256, 0, s>>>(d_sh, n, (uint32_t)depth, (uint32_t)sample, cfg->seed, last,
+            cbq_k_pt_shade<<<(n + 255) / 256, 256, 0, s>>>(d_sh, n, (uint32_t)depth, cfg->seed, last,
                                                           E.st, E.hit, E.material, E.position, E.normal, device_image,
                                                           so, sd, sw, counters, N.o, N.d, N.st, counters + 1);
             launches++;

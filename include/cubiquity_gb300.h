@@ -406,7 +406,9 @@ typedef struct cbq_pt_stats {
 } cbq_pt_stats;
 
 /* Called after every traversal wave with device pointers to its rays and hits
- * (kind 0: extension rays, 1: shadow rays); the stream has been synchronised. */
+ * (kind 0: extension rays, 1: shadow rays); the stream has been synchronised.
+ * A wave holds the paths of one pass: `sample` is the pass's first sample (a
+ * pass traces as many samples per pixel together as fit in 2^24 paths). */
 typedef void (*cbq_pt_wave_fn)(void* user, int32_t kind, int32_t depth, int32_t sample, const float* origin_tmax,
                                const float* direction, uint64_t n, const cbq_hits* hits, const cbq_query* query);
 
