@@ -114,8 +114,11 @@ __global__ void cbq_k_pt_camera(Frame f, float4* __restrict__ o, float4* __restr
     st[i] = PathState{pixel, sample, 1.0f, 1.0f, 1.0f};
 }
 
+// Contributions are never negative and the image starts at +0, so adding a zero
+// changes nothing: black contributions (most materials emit nothing) are skipped.
 __device__ __forceinline__ void add_pixel(float* image, uint32_t pixel, float r, float g, float b)
 {
+    if (r == 0.0f && g == 0.0f && b == 0.0f) return;
     atomicAdd(image + 3 * (size_t)pixel, r);
     atomicAdd(image + 3 * (size_t)pixel + 1, g);
     atomicAdd(image + 3 * (size_t)pixel + 2, b);
