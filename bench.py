@@ -595,7 +595,7 @@ def run_gpu_batch(args, world, rank, local):
     pinned_out = [{k: torch.from_numpy(v).pin_memory().numpy() for k, v in cbq.alloc_host_hits(o.shape[0]).items()
                    if k in ref_fields} for o, _ in pinned_in]
     server = cbq.Server(device_memory_budget=4 << 30, max_inflight_launches=8, max_batch_requests=64,
-                        max_batch_rays=2 << 20)
+                        max_batch_rays=1 << 20)
 
     def e2e_step():
         tickets = [server.submit(g, po, pd, queries_batch, out=out)[0]
