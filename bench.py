@@ -1,7 +1,8 @@
 """Benchmark: sparse-voxel-DAG ray traversal throughput on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload terrain-4096|spheres-256] [--kernel plain|persistent]
+                    [--workload terrain-4096|spheres-256|batch-64|serve-8|city-8192]
+                    [--form tuned|persistent|plain] [--no-extras]
 
 Workload (default terrain-4096): the seeded 4096^3 terrain DAG; one step traces
 4,194,304 primary rays (2048x2048 pinhole) and 4,194,304 cosine-weighted bounce
@@ -12,7 +13,16 @@ traversal's working set and stays in L2.
 
 `value` is device throughput (CUDA events on the launching stream); `e2e` is the
 same workload through the host-buffer C ABI (cbq_intersect_host) with pinned
-host rays in and hits out, copies inside the timed region.
+host rays in and hits out, copies inside the timed region.  `roofline` is that
+of the dominant launch against the L2 (the DAG is L2-resident; the same run
+measures the L2's read bandwidth and random-sector rate).  `fp64_error` compares
+the GPU's distances with the oracle's FP64 exact-box ray cast (CPU leg).
+
+On one GPU the default line also carries the benchmark's two other figures,
+measured after the terrain: `batch` (batch-64: the batched persistent launch
+against the plain drop-in launched once per volume) and `serve` (serve-8: peak
+request rate and p50/p99 latency at half of it, median of three runs, with the
+load generator's lateness).  `--no-extras` skips them.
 
 Multi-GPU (torchrun, N > 1): replicas only.  Rays are independent and the DAG is
 read-only, so every rank traces its own full replica; there is no data-path
@@ -61,6 +71,8 @@ def parse_args():
     p.add_argument("--chunk", type=int, default=0, help="persistent: refill threshold (flat) / grab size (nested)")
     p.add_argument("--e2e-steps", type=int, default=5)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="terrain-4096: skip the batch-64 and serve-8 measurements added to the line")
     p.add_argument("--layout", choices=["reference", "compact"], default="reference",
                    help="device node store: the reference's array, or the compact store (occupied children only)")
     p.add_argument("--serve-inflight", type=int, default=8, help="serve-8: launches in flight")
@@ -172,21 +184,19 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(workload: str):
-    """DRAM bytes per launch from the committed ncu summary, if one exists."""
+PROFILE_NOTE = "ncu capture committed in profiles/ (not this run)"
+
+
+def profiled_figure(workload: str, name: str, label: str | None = None):
+    """A figure of the committed ncu summary of this workload's traversal
+    (`name[label]: value` lines, e.g. `dram_bytes_per_ray[bounce]: 109.2`), or
+    None.  These come from an earlier ncu capture, never from the run that
+    prints them, and the bench line says so wherever it carries one."""
     f = ROOT / "profiles" / f"traverse_{workload}.md"
     if not f.exists():
         return None
-    m = re.search(r"dram_bytes_per_ray:\s*([0-9.]+)", f.read_text())
-    return float(m.group(1)) if m else None
-
-
-def profiled_issue_active(workload: str):
-    """smsp__issue_active (% of issue slots) of the traversal from the committed ncu summary."""
-    f = ROOT / "profiles" / f"traverse_{workload}.md"
-    if not f.exists():
-        return None
-    m = re.search(r"\| smsp__issue_active \| ([0-9.]+)%", f.read_text())
+    key = re.escape(name) + (r"\[" + re.escape(label) + r"\]" if label else "")
+    m = re.search(r"^" + key + r":\s*([0-9.]+)", f.read_text(), re.M)
     return float(m.group(1)) if m else None
 
 
@@ -382,27 +392,47 @@ def run_gpu(args, world, rank, local):
     launch_ms = {b[0]: float(np.mean([per_launch[k][i][0].elapsed_time(per_launch[k][i][1])
                                       for k in range(args.steps)])) for i, b in enumerate(dev_batches)}
 
-    # Roofline of the traversal kernel: algorithmic bytes per launch / launch time.
-    peak, peak_kind = measured_peaks()
-    alg_bytes = {b[0]: b[1].shape[0] * (RAY_BYTES + b[4] * SECTOR + HIT_BYTES) for b in dev_batches}
-    tot_bytes = sum(alg_bytes.values())
-    tot_ms = sum(launch_ms.values())
-    achieved = tot_bytes / (tot_ms * 1e-3) / 1e9
+    # Roofline of the dominant traversal launch.  Its node fetches are dependent
+    # 4-byte loads, one 32-byte L2 sector each, from a DAG that stays in L2: the
+    # bound is the L2, whose read bandwidth and random-sector rate this run
+    # measures itself (cbq_measure_l2).  Algorithmic bytes per ray = 32 (ray in)
+    # + F x 32 (one sector per node fetch) + 46 (hit record out).
+    hbm_peak, hbm_kind = measured_peaks()
     l2_stream, l2_rand = cbq.measure_l2(64 << 20, 20)
-    sectors = sum(b[1].shape[0] * b[4] for b in dev_batches)
-    sector_rate = sectors / (tot_ms * 1e-3) / 1e9
-    traffic_per_ray = profiled_traffic(args.workload)
+    per_batch = {}
+    for label, to, _, _, f in dev_batches:
+        n = to.shape[0]
+        ms = launch_ms[label]
+        bpr = RAY_BYTES + f * SECTOR + HIT_BYTES
+        achieved = n * bpr / (ms * 1e-3) / 1e9
+        sectors = n * f / (ms * 1e-3) / 1e9
+        dram = profiled_figure(args.workload, "dram_bytes_per_ray", label)
+        c = tuned.get(label, cfg)
+        per_batch[label] = {
+            "rays": n, "launch_ms": ms, "fetches_per_ray": f, "bytes_per_ray": bpr,
+            "kernel": ("cbq_k_flat_r56" if c.get("registers") == 56 and c.get("form") != 0 and c.get("stack") == 1
+                       else kernel_name),
+            "achieved_gbs": achieved, "frac_l2_stream": achieved / l2_stream,
+            "sector_rate_gsps": sectors, "frac_l2_sector": sectors / l2_rand,
+            "dram_bytes_per_launch": None if dram is None else dram * n,
+            "frac_hbm": None if dram is None else dram * n / (ms * 1e-3) / 1e9 / hbm_peak}
+    dominant = max(launch_ms, key=launch_ms.get)
+    dom = per_batch[dominant]
+    issue = profiled_figure(args.workload, "issue_active_pct", dominant)
     roofline = {
-        "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-        "peak_source": f"{peak_kind} hbm_gbs", "kernel": kernel_name,
-        "traffic": None if traffic_per_ray is None else traffic_per_ray * rays_per_step / len(dev_batches),
-        "limiter": {"kind": "instruction issue (dependent node fetches are served from L2)",
-                    "issue_active_pct": profiled_issue_active(args.workload), "source": "ncu --set full"},
-        "bytes_per_ray": {b[0]: RAY_BYTES + b[4] * SECTOR + HIT_BYTES for b in dev_batches},
-        "fetches_per_ray": {b[0]: b[4] for b in dev_batches},
-        "l2": {"achieved_gbs": achieved, "stream_peak_gbs": l2_stream, "frac_stream": achieved / l2_stream,
-               "sector_rate_gsps": sector_rate, "random_sector_peak_gsps": l2_rand,
-               "frac_sector": sector_rate / l2_rand, "peak_source": "cbq_measure_l2 (this run)"},
+        "bound": "l2", "achieved": dom["achieved_gbs"], "peak": l2_stream, "unit": "GB/s",
+        "frac": dom["frac_l2_stream"], "traffic": dom["dram_bytes_per_launch"],
+        "kernel": dom["kernel"], "launch": f"{dominant} batch ({dom['rays']} rays, {dom['launch_ms']:.3f} ms per launch)",
+        "peak_source": "cbq_measure_l2 in this run: streaming reads of a 64 MB L2-resident buffer",
+        "traffic_source": f"dram__bytes_read.sum + dram__bytes_write.sum per launch, {PROFILE_NOTE}",
+        "sector": {"achieved_gsps": dom["sector_rate_gsps"], "peak_gsps": l2_rand, "frac": dom["frac_l2_sector"],
+                   "peak_source": "cbq_measure_l2 in this run: independent random 32-byte sector reads"},
+        "hbm": {"frac": dom["frac_hbm"], "peak_gbs": hbm_peak, "peak_source": f"{hbm_kind} hbm_gbs",
+                "note": "DRAM traffic of the launch (the ray and hit streams plus node-store misses) over its time; "
+                        "traffic from the ncu capture, time from this run"},
+        "limiter": {"kind": "instruction issue (the node fetches hit in L2)", "issue_active_pct": issue,
+                    "source": PROFILE_NOTE},
+        "per_batch": per_batch,
     }
 
     # End to end through the host-buffer C ABI, pinned host memory, copies inside.
@@ -437,11 +467,13 @@ def run_gpu(args, world, rank, local):
     e2e_value = rays_per_step * args.e2e_steps * world / e2e_s / 1e6
 
     cpu = None
+    fp64 = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         dt, kind = cpu_trace(nodes, root, batches)
         cores = host_cores()
         cpu = {"value": rays_per_step / dt / 1e6, "unit": "Mrays/s", "cores": cores, "cpu": host_cpu(), "kind": kind,
                "sample": f"one pass over the full workload ({rays_per_step} rays), {cores} host threads"}
+        fp64 = fp64_error(nodes, root, batches, [b[3] for b in dev_batches])
 
     launches = args.steps * len(dev_batches)
     line = {
@@ -468,10 +500,52 @@ def run_gpu(args, world, rank, local):
                 "fields": "hit, distance, material, position, normal (the reference's RayVolumeIntersection)"},
         "gpu_launches": launches,
         "clocks": clk,
+        "fp64_error": fp64,
     }
+    dag.destroy()
+    # BASELINE's other two measurements, on the same GPU after this one: the
+    # batched form against the plain drop-in (batch-64) and the serving latency
+    # (serve-8).  Single-GPU runs only.
+    if world == 1 and args.workload == "terrain-4096" and not args.no_extras:
+        line["batch"] = measure_batch(args, world, local, e2e_steps=3)[0]
+        line["serve"] = measure_serve(args, world, local, sweep=False)[0]
     if rank == 0:
         print(json.dumps(line), flush=True)
-    dag.destroy()
+
+
+def fp64_error(nodes, root, batches, gpu_outs) -> dict:
+    """The GPU's FP32 hit records against the oracle's FP64 exact-box ray cast
+    (the reference's own check compares intersectVolume with traceRayRef,
+    test_rendering.cpp:75-80).  Per batch: hit and material disagreements and
+    the relative distance error |d32 - d64| / max(d64, 1 voxel) over rays both
+    hit, with the rays above 1e-5 (grazing rays: an edge or corner decided the
+    other way in FP32) counted and listed.  Part of the CPU leg."""
+    import oracle
+
+    orc = oracle.Oracle()
+    sd = orc.find_subdags(nodes, root)
+    out = {}
+    for (label, o, d), g in zip(batches, gpu_outs):
+        exact = orc.trace_fp64(nodes, sd, o, d)
+        hit = g["hit"].cpu().numpy().astype(bool)
+        dist = g["distance"].cpu().numpy().astype(np.float64)
+        mat = g["material"].cpu().numpy().astype(np.uint32)
+        ehit = exact["hit"].astype(bool)
+        both = hit & ehit
+        rel = np.abs(dist[both] - exact["distance"][both]) / np.maximum(np.abs(exact["distance"][both]), 1.0)
+        idx = np.nonzero(both)[0]
+        over = idx[rel > 1e-5]
+        hit_mm = np.nonzero(hit != ehit)[0]
+        mat_mm = np.nonzero(both & (mat != exact["material"]))[0]
+        out[label] = {"rays": int(o.shape[0]), "hits": int(hit.sum()), "hit_mismatches": int(hit_mm.size),
+                      "hit_mismatch_rays": hit_mm[:20].tolist(), "material_mismatches": int(mat_mm.size),
+                      "material_mismatch_rays": mat_mm[:20].tolist(),
+                      "rel_p50": float(np.quantile(rel, 0.5)) if rel.size else None,
+                      "rel_p999": float(np.quantile(rel, 0.999)) if rel.size else None,
+                      "rel_max": float(rel.max()) if rel.size else None,
+                      "over_1e-5": int(over.size), "over_1e-5_rays": over[:20].tolist()}
+    return {"batches": out, "oracle": "orc_trace_fp64_batch: exact voxel boxes, double precision",
+            "tolerance": "1e-5 relative (distance; grazing rays above it are counted and listed)"}
 
 
 def batch_jobs():
@@ -527,9 +601,11 @@ def run_reference_batch(args, world, rank):
         "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}), flush=True)
 
 
-def run_gpu_batch(args, world, rank, local):
+def measure_batch(args, world, local, e2e_steps: int | None = None):
     """batch-64: many volumes of uneven size in one persistent, graph-captured,
-    autotuned launch, against the plain kernel launched once per volume."""
+    autotuned launch, against the plain drop-in launched once per volume.
+    Returns (summary, details): the summary is what the default line carries
+    under `batch`; the details make the full `--workload batch-64` line."""
     import torch
     import cubiquity_gb300 as cbq
 
@@ -542,6 +618,7 @@ def run_gpu_batch(args, world, rank, local):
     plain_out = [cbq.alloc_hits(o.shape[0]) for o, _ in dev]
     batch = cbq.Batch([(g, o, d) for g, (o, d) in zip(dags, dev)])
     tuned = batch.autotune(3, stream=stream)
+    steps = max(3, args.steps)
 
     def plain_step():
         for g, (o, d), out in zip(dags, dev, plain_out):
@@ -550,7 +627,7 @@ def run_gpu_batch(args, world, rank, local):
     def batched_step():
         batch.launch(stream=stream)
 
-    def timed(fn, steps):
+    def timed(fn):
         for _ in range(max(3, args.warmup)):
             fn()
         torch.cuda.synchronize()
@@ -565,26 +642,27 @@ def run_gpu_batch(args, world, rank, local):
         barrier(world)
         return max_over_ranks(world, e0.elapsed_time(e1))
 
-    plain_ms = timed(plain_step, args.steps)
+    plain_ms = timed(plain_step)
     clocks = ClockSampler(local)
     clocks.start()
-    batched_ms = timed(batched_step, args.steps)
+    batched_ms = timed(batched_step)
     clk = clocks.stop()
     # Same answers from both forms.
     for out_b, out_p in zip(batch.outputs, plain_out):
         for k in ("hit", "material", "voxel", "distance", "status"):
             if not torch.equal(out_b[k], out_p[k]):
                 raise SystemExit(f"batched and plain results differ in {k}")
-    value = rays_per_step * args.steps * world / (batched_ms * 1e-3) / 1e6
-    plain_value = rays_per_step * args.steps * world / (plain_ms * 1e-3) / 1e6
+    value = rays_per_step * steps * world / (batched_ms * 1e-3) / 1e6
+    plain_value = rays_per_step * steps * world / (plain_ms * 1e-3) / 1e6
 
-    # Roofline of the batched launch.
+    # Roofline of the batched launch (algorithmic bytes as for the single-volume launch).
     fetches = sum(cbq.count_fetches(g, o, d).double().sum().item() for g, (o, d) in zip(dags, dev))
-    peak, peak_kind = measured_peaks()
-    step_s = batched_ms / args.steps * 1e-3
+    hbm_peak, hbm_kind = measured_peaks()
+    step_s = batched_ms / steps * 1e-3
     alg_bytes = rays_per_step * (RAY_BYTES + HIT_BYTES) + fetches * SECTOR
     achieved = alg_bytes / step_s / 1e9
     l2_stream, l2_rand = cbq.measure_l2(64 << 20, 20)
+    dram = profiled_figure("batch-64", "dram_bytes_per_ray")
 
     # End to end from host buffers: each step submits the 64 volumes' pinned rays to the request
     # server as one request each and waits for all hits (the reference's result fields) in host
@@ -596,6 +674,7 @@ def run_gpu_batch(args, world, rank, local):
                    if k in ref_fields} for o, _ in pinned_in]
     server = cbq.Server(device_memory_budget=4 << 30, max_inflight_launches=8, max_batch_requests=64,
                         max_batch_rays=1 << 20)
+    queries_batch = cbq.Query()
 
     def e2e_step():
         tickets = [server.submit(g, po, pd, queries_batch, out=out)[0]
@@ -603,69 +682,100 @@ def run_gpu_batch(args, world, rank, local):
         for t_ in tickets:
             server.wait(t_)
 
-    queries_batch = cbq.Query()
+    n_e2e = e2e_steps if e2e_steps is not None else args.e2e_steps
     e2e_step()
     server.reset_stats()
     t = time.perf_counter()
-    for _ in range(args.e2e_steps):
+    for _ in range(n_e2e):
         e2e_step()
-    e2e_value = rays_per_step * args.e2e_steps * world / max_over_ranks(world, time.perf_counter() - t) / 1e6
+    e2e_value = rays_per_step * n_e2e * world / max_over_ranks(world, time.perf_counter() - t) / 1e6
     e2e_launches = server.stats()["launches"]
     server.close()
+    batch.destroy()
+    for g in dags:
+        g.destroy()
 
+    summary = {
+        "workload": "batch-64", "volumes": len(dags), "rays_per_step": rays_per_step, "steps": steps,
+        "batched_mrays": value, "plain_mrays": plain_value, "batched_over_plain": value / plain_value,
+        "batched_ms_per_step": batched_ms / steps, "plain_ms_per_step": plain_ms / steps,
+        "batched_form": "one persistent cbq_k_flat_batch launch per step, replayed from a CUDA graph, autotuned",
+        "plain_form": "the drop-in cbq_intersect once per volume (64 launches per step)",
+        "batch_config": tuned, "fetches_per_ray": fetches / rays_per_step,
+        "l2_frac_stream": achieved / l2_stream,
+        "e2e_mrays": e2e_value, "clocks": clk,
+    }
+    details = {
+        "rays_per_step": rays_per_step, "steps": steps, "value": value, "ms_per_step": batched_ms / steps, "clk": clk,
+        "dag_bytes": int(sum(g.bytes for g in dags)), "device_node_bytes": int(sum(g.device_bytes for g in dags)),
+        "tuned": tuned, "plain_value": plain_value, "plain_ms": plain_ms / steps,
+        "roofline": {"bound": "l2", "achieved": achieved, "peak": l2_stream, "unit": "GB/s",
+                     "frac": achieved / l2_stream, "kernel": "cbq_k_flat_batch",
+                     "peak_source": "cbq_measure_l2 in this run: streaming reads of a 64 MB L2-resident buffer",
+                     "traffic": None if dram is None else dram * rays_per_step,
+                     "traffic_source": f"dram__bytes_read.sum + dram__bytes_write.sum per launch, {PROFILE_NOTE}",
+                     "fetches_per_ray": fetches / rays_per_step,
+                     "sector": {"achieved_gsps": fetches / step_s / 1e9, "peak_gsps": l2_rand,
+                                "frac": fetches / step_s / 1e9 / l2_rand},
+                     "hbm": {"frac": None if dram is None else dram * rays_per_step / step_s / 1e9 / hbm_peak,
+                             "peak_gbs": hbm_peak, "peak_source": f"{hbm_kind} hbm_gbs"},
+                     "limiter": {"kind": "instruction issue",
+                                 "issue_active_pct": profiled_figure("batch-64", "issue_active_pct"),
+                                 "source": PROFILE_NOTE}},
+        "e2e": e2e_value, "e2e_launches_per_step": e2e_launches / max(1, n_e2e), "e2e_steps": n_e2e,
+    }
+    return summary, details
+
+
+def run_gpu_batch(args, world, rank, local):
+    """The full bench line of batch-64 (`--workload batch-64`)."""
+    s, d = measure_batch(args, world, local)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         import oracle
         orc = oracle.Oracle()
         t0 = time.perf_counter()
-        for n, r, o, d in host_jobs:
-            orc.intersect(n, orc.find_subdags(n, r), o, d)
+        for n, r, o, dd in batch_jobs():
+            orc.intersect(n, orc.find_subdags(n, r), o, dd)
         dt = time.perf_counter() - t0
-        cpu = {"value": rays_per_step / dt / 1e6, "unit": "Mrays/s", "cores": host_cores(), "cpu": host_cpu(), "kind": "port",
-               "sample": f"one pass over all 64 volumes ({rays_per_step} rays), {host_cores()} host threads"}
-    batch_traffic = profiled_traffic("batch-64")  # DRAM bytes per ray, one launch (ncu)
+        cpu = {"value": d["rays_per_step"] / dt / 1e6, "unit": "Mrays/s", "cores": host_cores(), "cpu": host_cpu(),
+               "kind": "port", "sample": f"one pass over all 64 volumes ({d['rays_per_step']} rays), "
+                                         f"{host_cores()} host threads"}
     line = {
-        "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
-        "warmup": max(3, args.warmup), "ms_per_step": batched_ms / args.steps, "higher_is_better": True,
+        "metric": "Mrays/s", "value": d["value"], "unit": "Mrays/s", "n_gpus": world, "steps": d["steps"],
+        "warmup": max(3, args.warmup), "ms_per_step": d["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (64 seeded sphere/terrain volumes, edges 2^7..2^11, generated rays)",
-        "config": {"workload": "batch-64", "volumes": len(dags), "rays_per_step": rays_per_step,
-                   "dag_bytes": int(sum(g.bytes for g in dags)), "layout": args.layout,
-                   "device_node_bytes": int(sum(g.device_bytes for g in dags)), "batch_config": tuned,
-                   "form": "one persistent launch replayed from a CUDA graph",
-                   "l2": "inputs larger than L2 (rays + hits %.0f MB per step)" % (rays_per_step * 78 / 1e6)},
-        "plain": {"value": plain_value, "unit": "Mrays/s", "ms_per_step": plain_ms / args.steps,
+        "config": {"workload": "batch-64", "volumes": s["volumes"], "rays_per_step": d["rays_per_step"],
+                   "dag_bytes": d["dag_bytes"], "layout": args.layout, "device_node_bytes": d["device_node_bytes"],
+                   "batch_config": d["tuned"], "form": "one persistent launch replayed from a CUDA graph",
+                   "l2": "inputs larger than L2 (rays + hits %.0f MB per step)" % (d["rays_per_step"] * 78 / 1e6)},
+        "plain": {"value": d["plain_value"], "unit": "Mrays/s", "ms_per_step": d["plain_ms"],
                   "form": "cbq_intersect once per volume (64 launches per step)"},
-        "batched_over_plain": value / plain_value,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": f"{peak_kind} hbm_gbs", "kernel": "cbq_k_flat_batch",
-                     "traffic": None if batch_traffic is None else batch_traffic * rays_per_step,
-                     "limiter": {"kind": "instruction issue", "issue_active_pct": profiled_issue_active("batch-64"),
-                                 "source": "ncu --set full"},
-                     "fetches_per_ray": fetches / rays_per_step,
-                     "l2": {"stream_peak_gbs": l2_stream, "frac_stream": achieved / l2_stream,
-                            "sector_rate_gsps": fetches / step_s / 1e9, "random_sector_peak_gsps": l2_rand}},
+        "batched_over_plain": d["value"] / d["plain_value"],
+        "roofline": d["roofline"],
         "cpu_baseline": cpu,
-        "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": rays_per_step * RAY_BYTES,
-                "d2h_bytes_per_step": rays_per_step * REF_HIT_BYTES,
+        "e2e": {"value": d["e2e"], "unit": "Mrays/s", "h2d_bytes_per_step": d["rays_per_step"] * RAY_BYTES,
+                "d2h_bytes_per_step": d["rays_per_step"] * REF_HIT_BYTES,
                 "api": "cbq_server_submit/wait, one request per volume (pinned host buffers)",
                 "fields": "hit, distance, material, position, normal (the reference's RayVolumeIntersection)",
-                "launches_per_step": e2e_launches / args.e2e_steps},
-        "gpu_launches": args.steps,
-        "clocks": clk,
+                "launches_per_step": d["e2e_launches_per_step"]},
+        "gpu_launches": d["steps"],
+        "clocks": d["clk"],
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
 
 
-def run_gpu_serve(args, world, rank, local):
+def measure_serve(args, world, local, half_runs: int = 3, half_seconds: float = 4.0, sweep: bool = True):
     """serve-8: 8 resident terrain DAGs (edges 1024-4096); requests of 1k-256k
     rays (log-uniform), 70% tmax-bounded collision rays and 30% view rays.
     Finds the peak request rate closed-loop, then drives an open-loop Poisson
     stream at half of it and reports p50/p99 latency (submit -> hits in host
-    memory, timed by the server) and Mrays/s."""
+    memory, timed by the server) and Mrays/s, with the generator's own
+    lateness (actual submit time minus scheduled arrival) beside them.
+    Returns (summary, details)."""
     import random
-    import threading
     import torch
     import cubiquity_gb300 as cbq
     from cubiquity_gb300 import workloads as W
@@ -673,6 +783,7 @@ def run_gpu_serve(args, world, rank, local):
     # The generator spins on the clock while the waiter thread blocks in the
     # library: a short switch interval keeps the spinning thread from holding
     # the GIL for whole 5 ms slices, which would make arrivals bursty.
+    old_interval = sys.getswitchinterval()
     sys.setswitchinterval(5e-5)
     torch.cuda.set_device(local)
     scenes = W.serve_volumes()
@@ -693,9 +804,8 @@ def run_gpu_serve(args, world, rank, local):
              "voxel": torch.empty((max_n, 3), dtype=torch.int32).pin_memory().numpy(),
              "status": torch.empty(max_n, dtype=torch.uint8).pin_memory().numpy()} for _ in range(ring)]
     in_place = args.serve_buffers == "in-place"
-    server = cbq.Server(device_memory_budget=2 << 30, max_inflight_launches=args.serve_inflight,
-                        max_batch_requests=128, max_batch_rays=args.serve_batch_rays, in_place=in_place)
     queries = {True: cbq.Query(True, cbq.MAX_FOOTPRINT_DISABLED, True), False: cbq.Query()}
+    server = None
 
     def submit(k, r):
         (co, cd), (vo, vd) = pools[r.volume]
@@ -717,18 +827,23 @@ def run_gpu_serve(args, world, rank, local):
             server.wait(t)
         return time.perf_counter() - t0
 
-    n_peak = 3000
-    # The same closed loop through a server of the other buffer mode.
-    live = server
-    server = cbq.Server(device_memory_budget=2 << 30, max_inflight_launches=args.serve_inflight,
-                        max_batch_requests=128, max_batch_rays=args.serve_batch_rays, in_place=not in_place)
-    closed_loop(0, 300)
-    server.reset_stats()
-    dt_other = closed_loop(300, n_peak)
-    other = server.stats()
-    server.close()
-    server = live
+    def make_server(place):
+        return cbq.Server(device_memory_budget=2 << 30, max_inflight_launches=args.serve_inflight,
+                          max_batch_requests=128, max_batch_rays=args.serve_batch_rays, in_place=place)
 
+    n_peak = 3000
+    other = None
+    if sweep:  # the same closed loop through a server of the other buffer mode
+        server = make_server(not in_place)
+        closed_loop(0, 300)
+        server.reset_stats()
+        dt_other = closed_loop(300, n_peak)
+        st = server.stats()
+        other = {"buffers": "staged" if in_place else "in-place", "requests_per_s": n_peak / dt_other,
+                 "mrays_per_s": st["rays_completed"] / dt_other / 1e6, "p50_ms": st["latency_p50_us"] / 1e3,
+                 "p99_ms": st["latency_p99_us"] / 1e3}
+        server.close()
+    server = make_server(in_place)
     closed_loop(0, 300)  # warm-up
     server.reset_stats()
     dt = closed_loop(300, n_peak)
@@ -744,8 +859,8 @@ def run_gpu_serve(args, world, rank, local):
             t += rng.expovariate(rate)
             times.append(t)
         tickets = [None] * len(times)
+        late = np.zeros(len(times))
         done = threading.Semaphore(ring)
-        issued = threading.Event()
 
         def waiter():
             for i in range(len(times)):
@@ -765,6 +880,7 @@ def run_gpu_serve(args, world, rank, local):
             if not done.acquire(blocking=False):
                 backpressure += 1
                 done.acquire()
+            late[i] = time.perf_counter() - t0 - at
             tickets[i] = submit(first + i, reqs[(first + i) % len(reqs)])
         th.join()
         wall = time.perf_counter() - t0
@@ -773,41 +889,64 @@ def run_gpu_serve(args, world, rank, local):
                 "p99_ms": st["latency_p99_us"] / 1e3, "max_ms": st["latency_max_us"] / 1e3,
                 "mrays_per_s": st["rays_completed"] / wall / 1e6, "requests_per_launch": st["mean_requests_per_launch"],
                 "generator_backpressure": backpressure, "direct_requests": st["direct_requests"],
-                "launches": st["launches"]}
+                "launches": st["launches"],
+                "generator_lateness_ms": {"p50": float(np.quantile(late, 0.5)) * 1e3,
+                                          "p99": float(np.quantile(late, 0.99)) * 1e3,
+                                          "max": float(late.max()) * 1e3}}
 
     clocks = ClockSampler(local)
     clocks.start()
-    # Three 4 s runs at half load; the line reports the run with the median p99
+    # `half_runs` runs at half load; the result is the run with the median p99
     # (host jitter from other work on the machine moves single-run tails).
     import gc
     gc.collect()
     gc.disable()  # no collector pauses in the Python load generator while it runs
-    halves = [open_loop(0.5 * peak_rps, 4.0, 5000 + 40000 * k) for k in range(3)]
+    halves = [open_loop(0.5 * peak_rps, half_seconds, 5000 + 40000 * k) for k in range(half_runs)]
     clk = clocks.stop()
-    half = dict(sorted(halves, key=lambda r: r["p99_ms"])[1])
+    half = dict(sorted(halves, key=lambda r: r["p99_ms"])[len(halves) // 2])
     half["p99_ms_runs"] = [r["p99_ms"] for r in halves]
-    sweep = [open_loop(f * peak_rps, 2.0, 9000 + int(f * 1000)) for f in (0.25, 0.75)]
+    sweep_runs = [open_loop(f * peak_rps, 2.0, 9000 + int(f * 1000)) for f in (0.25, 0.75)] if sweep else []
     gc.enable()
     server.close()
+    for g in dags:
+        g.destroy()
+    sys.setswitchinterval(old_interval)
+    buffers = "page-locked host, served in place" if in_place else "page-locked host, staged through device memory"
+    summary = {
+        "workload": "serve-8", "edges": [1 << s.edge_log2 for s in scenes],
+        "peak_requests_per_s": peak_rps, "peak_mrays_per_s": peak_mrays,
+        "half_load": {"rate_rps": half["rate_rps"], "p50_ms": half["p50_ms"], "p99_ms": half["p99_ms"],
+                      "p99_ms_runs": half["p99_ms_runs"], "seconds_per_run": half_seconds,
+                      "mrays_per_s": half["mrays_per_s"], "requests_per_launch": half["requests_per_launch"],
+                      "generator_lateness_ms": half["generator_lateness_ms"]},
+        "latency": "submit -> hits in host memory, timed by the server; p99 = median over the runs",
+        "arrivals": "open-loop Poisson from a Python generator", "buffers": buffers, "clocks": clk,
+    }
+    details = {"scenes": scenes, "in_place": in_place, "peak": peak, "peak_rps": peak_rps, "peak_mrays": peak_mrays,
+               "other": other, "half": half, "sweep": sweep_runs, "clk": clk, "buffers": buffers}
+    return summary, details
+
+
+def run_gpu_serve(args, world, rank, local):
+    """The full bench line of serve-8 (`--workload serve-8`)."""
+    s, d = measure_serve(args, world, local)
+    half, peak = d["half"], d["peak"]
     line = {
         "metric": "p99 latency at 50% of peak load", "value": half["p99_ms"], "unit": "ms", "n_gpus": world,
         "steps": half["requests"], "warmup": 300, "ms_per_step": half["p50_ms"], "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (8 seeded terrain DAGs, 1k-256k-ray requests: 70% collision tmax<=64, 30% view)",
-        "config": {"workload": "serve-8", "edges": [1 << s.edge_log2 for s in scenes],
+        "config": {"workload": "serve-8", "edges": s["edges"],
                    "server": {"memory_budget_gb": 2, "inflight_launches": args.serve_inflight,
                               "max_batch_requests": 128, "max_batch_rays": args.serve_batch_rays,
-                              "buffers": "page-locked host, served in place" if in_place else
-                              "page-locked host, staged through device memory"},
+                              "buffers": d["buffers"]},
                    "arrivals": "open-loop Poisson"},
-        "peak": {"requests_per_s": peak_rps, "mrays_per_s": peak_mrays, "p50_ms": peak["latency_p50_us"] / 1e3,
+        "peak": {"requests_per_s": d["peak_rps"], "mrays_per_s": d["peak_mrays"], "p50_ms": peak["latency_p50_us"] / 1e3,
                  "p99_ms": peak["latency_p99_us"] / 1e3, "direct_requests": peak["direct_requests"]},
-        "peak_other_buffers": {"buffers": "staged" if in_place else "in-place", "requests_per_s": n_peak / dt_other,
-                               "mrays_per_s": other["rays_completed"] / dt_other / 1e6,
-                               "p50_ms": other["latency_p50_us"] / 1e3, "p99_ms": other["latency_p99_us"] / 1e3},
-        "half_load": half, "sweep": sweep,
+        "peak_other_buffers": d["other"],
+        "half_load": half, "sweep": d["sweep"],
         "e2e": {"value": half["mrays_per_s"], "unit": "Mrays/s", "note": "host rays in, host hits out, per request"},
-        "gpu_launches": half["launches"], "clocks": clk,
+        "gpu_launches": half["launches"], "clocks": d["clk"],
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
