@@ -220,6 +220,18 @@ __global__ void __launch_bounds__(kPersistBlock) cbq_k_intersect_persistent(
     }
 }
 
+namespace {
+
+cbq_status preload_nested_persistent()
+{
+    cudaFuncAttributes a;
+    if (cudaFuncGetAttributes(&a, cbq_k_intersect_persistent) == cudaSuccess) return CBQ_OK;
+    cudaGetLastError();
+    return CBQ_ERR_CUDA;
+}
+
+}  // namespace
+
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
@@ -250,6 +262,12 @@ cbq_status cbq_dag_create_ex(const uint32_t* host_nodes, uint64_t node_count, ui
     for (int i = 0; i < 8; i++)
         if (dag->subdags[i].node_index > 0) dag->max_height = std::max(dag->max_height, dag->subdags[i].node_height);
     if (cudaGetDevice(&dag->device) != cudaSuccess) { delete dag; return CBQ_ERR_CUDA; }
+    // Materialise cbq_intersect_host_noalloc's fixed array, and load the persistent
+    // kernels it launches, on this device now, while allocating is expected, so that
+    // the no-allocation entry point never does (CUDA loads both lazily).
+    if (noalloc_prepare(dag->device) != CBQ_OK || preload_persistent_kernels() != CBQ_OK ||
+        preload_nested_persistent() != CBQ_OK)
+        cbq::log(CBQ_LOG_WARNING, "device %d: the no-allocation staging array could not be prepared", dag->device);
     for (int i = 0; i < 8; i++) dag->sd_ref[i] = dag->subdags[i].node_index;
     const uint32_t* src = host_nodes;
     size_t bytes = (size_t)node_count * 32u;

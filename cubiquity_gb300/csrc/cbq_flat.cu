@@ -161,6 +161,32 @@ bool float_positions_exact(const cbq_dag* dag)
 
 namespace {
 
+template <typename Ctx>
+bool query_persistent_kernels()
+{
+    cudaFuncAttributes a;
+    return cudaFuncGetAttributes(&a, dev::cbq_k_flat<true, false, false, Ctx>) == cudaSuccess &&
+           cudaFuncGetAttributes(&a, dev::cbq_k_flat<true, false, true, Ctx>) == cudaSuccess &&
+           cudaFuncGetAttributes(&a, dev::cbq_k_flat<true, true, false, Ctx>) == cudaSuccess &&
+           cudaFuncGetAttributes(&a, dev::cbq_k_flat<true, true, true, Ctx>) == cudaSuccess &&
+           cudaFuncGetAttributes(&a, dev::cbq_k_flat_r56<false, Ctx>) == cudaSuccess &&
+           cudaFuncGetAttributes(&a, dev::cbq_k_flat_r56<true, Ctx>) == cudaSuccess;
+}
+
+}  // namespace
+
+// Querying a kernel's attributes loads it on the current device (CUDA loads
+// modules and kernels lazily, on first use, and that load can take device
+// memory).  Done for every persistent traversal kernel when a DAG is created.
+cbq_status preload_persistent_kernels()
+{
+    const bool ok = query_persistent_kernels<dev::FlatCtxT<false>>() && query_persistent_kernels<dev::FlatCtxT<true>>();
+    if (!ok) cudaGetLastError();
+    return ok ? CBQ_OK : CBQ_ERR_CUDA;
+}
+
+namespace {
+
 template <bool P, bool S, bool O, typename Ctx>
 cbq_status launch_variant(const Ctx& c, uint64_t n, const FlatLaunch& fl, int rows, cudaStream_t stream,
                           int device)

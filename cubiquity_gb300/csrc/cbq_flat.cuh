@@ -350,4 +350,6 @@ cbq_status launch_flat(const cbq_dag* dag, const dev::DagParams& dp, const dev::
 cbq_status launch_octant_sort(const float4* dir, uint64_t n, uint32_t* counts16, uint32_t* perm, int device,
                               cudaStream_t stream);
 bool float_positions_exact(const cbq_dag* dag);
+// Loads every persistent flat traversal kernel on the current device.
+cbq_status preload_persistent_kernels();
 }  // namespace cbq

@@ -40,6 +40,13 @@ cbq_status validate_heights(const uint32_t* nodes, uint64_t node_count, const cb
 cbq_status build_compact(const uint32_t* nodes, uint64_t node_count, const cbq_subdag subdags[8],
                          std::vector<uint32_t>& store, uint32_t sd_ref[8]);
 
+// Resolves, on the current device, the device address of the fixed staging
+// array of cbq_intersect_host_noalloc.  The lookup loads the module that holds
+// the array, which is when the array takes its device memory; cbq_dag_create
+// calls this so that the allocation happens there, never inside a
+// cbq_intersect_host_noalloc call.
+cbq_status noalloc_prepare(int device);
+
 // cbq_intersect_host splits a call into at most kHostChunksMax chunks of at
 // least kHostChunkMin rays.
 constexpr uint64_t kHostChunksMax = 8;

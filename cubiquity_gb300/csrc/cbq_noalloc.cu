@@ -9,6 +9,11 @@
 // This entry point keeps its staging buffers and the persistent kernel's work
 // counter in one file-scope __device__ array instead, of fixed size: requests
 // of more than CBQ_NOALLOC_MAX_RAYS rays are refused with CBQ_ERR_CAPACITY.
+//
+// The array takes device memory when the module that holds it is loaded on a
+// device, which (with CUDA's lazy module loading) is the first lookup of its
+// address there.  cbq_dag_create does that lookup (noalloc_prepare), so the
+// array is in place before any call of this entry point can name a DAG.
 #include "cbq_internal.hpp"
 
 #include <cuda_runtime.h>
@@ -22,17 +27,17 @@ constexpr size_t kRayBytes = 32;                                       // two fl
 constexpr size_t kHitBytes = 1 + 4 + 4 + 12 + 12 + 12 + 1;             // all hit fields
 constexpr size_t kScratchBytes = kMaxRays * (kRayBytes + kHitBytes) + 256;
 
-// One array per device that loads the library, held until the process exits.
-// In host code this name is only a stand-in for the device symbol: its device
-// address comes from cudaGetSymbolAddress below.
+// One array per device on which a DAG was created, held until the process
+// exits.  In host code this name is only a stand-in for the device symbol: its
+// device address comes from cudaGetSymbolAddress below.
 static __device__ __align__(256) unsigned char g_cbq_noalloc_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_lock;
 void* g_scratch_addr[kMaxDevices] = {};
 
-// Device address of the scratch array on the current device, looked up once
-// per device (the device must be current).
+// Device address of the scratch array on `device`, which must be current;
+// looked up once per device.
 cbq_status scratch_address(int device, void** out)
 {
     if (device < 0 || device >= kMaxDevices) return CBQ_ERR_INVALID_ARGUMENT;
@@ -51,6 +56,16 @@ cbq_status scratch_address(int device, void** out)
 
 }  // namespace
 
+namespace cbq {
+
+cbq_status noalloc_prepare(int device)
+{
+    void* p = nullptr;
+    return scratch_address(device, &p);
+}
+
+}  // namespace cbq
+
 extern "C" cbq_status cbq_intersect_host_noalloc(const cbq_dag* dag, const float* host_origin_tmax,
                                                  const float* host_direction, uint64_t n, const cbq_query* query,
                                                  const cbq_hits* host_hits)
@@ -62,7 +77,7 @@ extern "C" cbq_status cbq_intersect_host_noalloc(const cbq_dag* dag, const float
     if (cudaGetDevice(&device) != cudaSuccess) return CBQ_ERR_CUDA;
     if (device != dag->device) return CBQ_ERR_INVALID_ARGUMENT;  // the DAG lives on another device
     void* base = nullptr;
-    cbq_status st = scratch_address(device, &base);
+    cbq_status st = scratch_address(device, &base);  // resolved when the DAG was created
     if (st != CBQ_OK) return st;
 
     // Carve the array: rays, hit fields, then the work counter.  Every region
@@ -83,9 +98,21 @@ extern "C" cbq_status cbq_intersect_host_noalloc(const cbq_dag* dag, const float
     dh.status = (uint8_t*)p; p += n;
     uint64_t* d_counter = (uint64_t*)(((uintptr_t)p + 7u) & ~(uintptr_t)7u);
 
-    cudaStream_t s = 0;
-    if (cudaMemcpyAsync(d_o, host_origin_tmax, n * 16, cudaMemcpyHostToDevice, s) != cudaSuccess) return CBQ_ERR_CUDA;
-    if (cudaMemcpyAsync(d_d, host_direction, n * 16, cudaMemcpyHostToDevice, s) != cudaSuccess) return CBQ_ERR_CUDA;
+    // The calling thread's per-thread stream: it needs no creation, and it does
+    // not wait for (or hold up) work on other streams the way the legacy default
+    // stream would.
+    const cudaStream_t s = cudaStreamPerThread;
+    // Once anything is queued, every return waits for it to end first, so the
+    // caller's buffers are not touched after the call returns, error or not.
+    auto drain = [&](cbq_status err) {
+        const bool ok = cudaStreamSynchronize(s) == cudaSuccess;
+        cudaGetLastError();
+        return ok ? err : CBQ_ERR_CUDA;
+    };
+    if (cudaMemcpyAsync(d_o, host_origin_tmax, n * 16, cudaMemcpyHostToDevice, s) != cudaSuccess)
+        return drain(CBQ_ERR_CUDA);
+    if (cudaMemcpyAsync(d_d, host_direction, n * 16, cudaMemcpyHostToDevice, s) != cudaSuccess)
+        return drain(CBQ_ERR_CUDA);
     cbq_hits launch = dh;
     if (!host_hits->hit) launch.hit = nullptr;
     if (!host_hits->distance) launch.distance = nullptr;
@@ -95,8 +122,10 @@ extern "C" cbq_status cbq_intersect_host_noalloc(const cbq_dag* dag, const float
     if (!host_hits->voxel) launch.voxel = nullptr;
     if (!host_hits->status) launch.status = nullptr;
     cbq_rays rays{d_o, d_d};
+    // Always the persistent form (whatever the DAG's launch form): its work
+    // counter lives in the array too.  Results are the same bits in every form.
     st = cbq_intersect_persistent(dag, &rays, n, query, &launch, d_counter, 0u, (cbq_stream_t)s);
-    if (st != CBQ_OK) return st;
+    if (st != CBQ_OK) return drain(st);
     struct Copy { void* dst; const void* src; size_t bytes; };
     const Copy copies[] = {
         {host_hits->hit, launch.hit, n}, {host_hits->distance, launch.distance, n * 4},
@@ -105,7 +134,8 @@ extern "C" cbq_status cbq_intersect_host_noalloc(const cbq_dag* dag, const float
         {host_hits->status, launch.status, n}};
     for (const Copy& c : copies) {
         if (!c.dst) continue;
-        if (cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess) return CBQ_ERR_CUDA;
+        if (cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+            return drain(CBQ_ERR_CUDA);
     }
-    return cudaStreamSynchronize(s) == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
+    return drain(CBQ_OK);
 }

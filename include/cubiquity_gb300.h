@@ -247,17 +247,24 @@ cbq_status cbq_intersect_host(const cbq_dag* dag, const float* host_origin_tmax,
  * and stall every stream), or a host application whose own allocator owns all
  * device memory.  Rays and hits are staged, and the persistent kernel's work
  * counter kept, in one fixed array compiled into the library
- * (CBQ_NOALLOC_MAX_RAYS * 78 bytes + 256, about 5 MB, held on every device that
- * loads the library until the process exits).
+ * (CBQ_NOALLOC_MAX_RAYS * 78 bytes + 256, about 5 MB per device).
+ *   - The array takes its device memory when cbq_dag_create first runs on a
+ *     device: it loads the array's module there and looks up its address
+ *     (cudaGetSymbolAddress).  It is held until the process exits.  A call of
+ *     this entry point needs a DAG, so its array is always in place already;
+ *     the call itself allocates nothing, not even on its first use.
  *   - n > CBQ_NOALLOC_MAX_RAYS returns CBQ_ERR_CAPACITY; nothing is launched.
- *   - The current device must be the DAG's device.  The first call on a device
- *     looks up the array's device address (cudaGetSymbolAddress); make that
- *     first call before any stream capture.
+ *   - The current device must be the DAG's device.
+ *   - Copies and the launch go on the calling thread's per-thread stream
+ *     (cudaStreamPerThread), so the call neither waits for nor holds up other
+ *     streams.  It always runs the persistent form (same results as every
+ *     other form, whatever the DAG's launch configuration says).
  *   - Every call on a device shares the array and leaves its contents behind;
  *     each call rewrites what it reads (rays, hits) and zeroes the counter.
  *     Calls that overlap on the GPU (for instance from several host threads)
  *     race on the array: callers must serialise them.
- *   - Synchronous, like cbq_intersect_host. */
+ *   - Synchronous, like cbq_intersect_host: whether it succeeds or fails,
+ *     every copy and launch it queued has ended when it returns. */
 #define CBQ_NOALLOC_MAX_RAYS 65536u
 cbq_status cbq_intersect_host_noalloc(const cbq_dag* dag, const float* host_origin_tmax,
                                       const float* host_direction, uint64_t n, const cbq_query* query,
