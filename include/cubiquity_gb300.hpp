@@ -11,6 +11,10 @@
 //   cbq::Volume gpu(nodes_ptr, node_count, root);        // uploads once (SSBO-0 equivalent)
 //   cbq::RayVolumeIntersection r = cbq::intersectVolume(gpu, gpu.subDAGs(), ox, oy, oz, dx, dy, dz, true);
 //
+// Both of the reference's overloads are here (six floats, raytracing.h:72-75;
+// Ray3f, raytracing.h:77).  The SubDAGs passed must be the volume's own (those
+// of findSubDAGs on the same nodes and root); others raise cbq::Error.
+//
 // The single-ray overload exists for API compatibility (collision picking,
 // viewer.cpp:152-163); throughput callers use intersectVolumes() on batches.
 // Errors surface as cbq::Error exceptions on the C++ side only; the C ABI below
@@ -31,6 +35,16 @@ namespace cbq {
 struct vec3 {
     float x, y, z;
 };
+
+// The reference's Ray3f (geometry.h:229-250, Ray3<vec3f>): origin then
+// direction, 24 bytes.
+struct Ray3f {
+    vec3 mOrigin;
+    vec3 mDir;
+    Ray3f() = default;
+    Ray3f(const vec3& origin, const vec3& dir) : mOrigin(origin), mDir(dir) {}
+};
+static_assert(sizeof(Ray3f) == 24, "layout must match the reference");
 
 // Byte layout identical to the reference's RayVolumeIntersection (48 bytes:
 // bool hit @0, double distance @8, uint material @16, vec3 position @20,
@@ -130,19 +144,48 @@ inline void intersectVolumes(const Volume& volume, const float* origins_xyz, con
     }
 }
 
-// intersectVolume (raytracing.h:72-75), one ray.  `subDAGs` must be the
-// volume's own SubDAGs; it is accepted for signature compatibility.
+// True when `a` holds the same SubDAGs as `b` (lower bound, height and root
+// node of all eight; padding ignored).
+inline bool sameSubDAGs(const SubDAGArray& a, const SubDAGArray& b)
+{
+    for (int i = 0; i < 8; i++) {
+        const SubDAG& x = a[i];
+        const SubDAG& y = b[i];
+        if (x.lower_bound[0] != y.lower_bound[0] || x.lower_bound[1] != y.lower_bound[1] ||
+            x.lower_bound[2] != y.lower_bound[2] || x.node_height != y.node_height || x.node_index != y.node_index)
+            return false;
+    }
+    return true;
+}
+
+// intersectVolume (raytracing.h:77), one ray given as a Ray3f.  The device
+// traverses with the SubDAGs the volume computed when it was uploaded, which
+// equal findSubDAGs of the same nodes and root; SubDAGs of anything else (a
+// different root, an older version of the volume) are refused with
+// cbq::Error(CBQ_ERR_INVALID_ARGUMENT) rather than silently replaced.
+inline RayVolumeIntersection intersectVolume(const Volume& volume, const SubDAGArray& subDAGs, Ray3f ray,
+                                             bool computeSurfaceProperties,
+                                             float maxFootprint = MAX_FOOTPRINT_DISABLED)
+{
+    if (!sameSubDAGs(subDAGs, volume.subDAGs()))
+        throw Error(CBQ_ERR_INVALID_ARGUMENT, "intersectVolume: the SubDAGs are not this volume's");
+    const float o[3] = {ray.mOrigin.x, ray.mOrigin.y, ray.mOrigin.z};
+    const float d[3] = {ray.mDir.x, ray.mDir.y, ray.mDir.z};
+    RayVolumeIntersection r;
+    intersectVolumes(volume, o, d, 1, computeSurfaceProperties, maxFootprint, &r);
+    return r;
+}
+
+// intersectVolume (raytracing.h:72-76), one ray as six floats: forwards to the
+// Ray3f form, as the reference does (raytracing.cpp:397-405).
 inline RayVolumeIntersection intersectVolume(const Volume& volume, const SubDAGArray& subDAGs, float ray_orig_x,
                                              float ray_orig_y, float ray_orig_z, float ray_dir_x, float ray_dir_y,
                                              float ray_dir_z, bool computeSurfaceProperties,
                                              float maxFootprint = MAX_FOOTPRINT_DISABLED)
 {
-    (void)subDAGs;
-    const float o[3] = {ray_orig_x, ray_orig_y, ray_orig_z};
-    const float d[3] = {ray_dir_x, ray_dir_y, ray_dir_z};
-    RayVolumeIntersection r;
-    intersectVolumes(volume, o, d, 1, computeSurfaceProperties, maxFootprint, &r);
-    return r;
+    return intersectVolume(volume, subDAGs,
+                           Ray3f(vec3{ray_orig_x, ray_orig_y, ray_orig_z}, vec3{ray_dir_x, ray_dir_y, ray_dir_z}),
+                           computeSurfaceProperties, maxFootprint);
 }
 
 }  // namespace cbq
