@@ -69,7 +69,7 @@ def parse_args():
                         "pulling rays from a work counter; plain: one thread per ray")
     p.add_argument("--block", type=int, default=0)
     p.add_argument("--chunk", type=int, default=0, help="persistent: refill threshold (flat) / grab size (nested)")
-    p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--e2e-steps", type=int, default=20)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true",
                    help="terrain-4096: skip the batch-64 and serve-8 measurements added to the line")
@@ -770,21 +770,17 @@ def run_gpu_batch(args, world, rank, local):
 def measure_serve(args, world, local, half_runs: int = 3, half_seconds: float = 4.0, sweep: bool = True):
     """serve-8: 8 resident terrain DAGs (edges 1024-4096); requests of 1k-256k
     rays (log-uniform), 70% tmax-bounded collision rays and 30% view rays.
-    Finds the peak request rate closed-loop, then drives an open-loop Poisson
-    stream at half of it and reports p50/p99 latency (submit -> hits in host
-    memory, timed by the server) and Mrays/s, with the generator's own
-    lateness (actual submit time minus scheduled arrival) beside them.
-    Returns (summary, details)."""
-    import random
+    The load comes from the library's native trace driver (cbq_server_replay),
+    so the client's own timing is not the Python interpreter's: the peak
+    request rate is found closed loop (every arrival at time 0, 64 requests
+    outstanding), then an open-loop Poisson stream at half of it gives p50/p99
+    latency (submit -> hits in host memory, timed by the server) and Mrays/s,
+    with the driver's lateness (actual submit time minus scheduled arrival)
+    beside them.  Returns (summary, details)."""
     import torch
     import cubiquity_gb300 as cbq
     from cubiquity_gb300 import workloads as W
 
-    # The generator spins on the clock while the waiter thread blocks in the
-    # library: a short switch interval keeps the spinning thread from holding
-    # the GIL for whole 5 ms slices, which would make arrivals bursty.
-    old_interval = sys.getswitchinterval()
-    sys.setswitchinterval(5e-5)
     torch.cuda.set_device(local)
     scenes = W.serve_volumes()
     dags, pools = [], []
@@ -796,6 +792,16 @@ def measure_serve(args, world, local, half_runs: int = 3, half_seconds: float = 
         pools.append(((pin(co), pin(cd)), (pin(vo), pin(vd))))
     sizes = (1 << 19, 724 * 724)
     reqs = W.serve_requests(20000, sizes, seed=1234)
+    r_vol = np.array([r.volume for r in reqs])
+    r_coll = np.array([r.collision for r in reqs])
+    r_start = np.array([r.start for r in reqs], np.uint64)
+    r_count = np.array([r.count for r in reqs], np.uint64)
+    ptr = lambda a: a.ctypes.data  # noqa: E731
+    dag_h = np.array([g.handle.value for g in dags], np.uint64)
+    o_ptr = {True: np.array([ptr(p[0][0]) for p in pools], np.uint64),
+             False: np.array([ptr(p[1][0]) for p in pools], np.uint64)}
+    d_ptr = {True: np.array([ptr(p[0][1]) for p in pools], np.uint64),
+             False: np.array([ptr(p[1][1]) for p in pools], np.uint64)}
     ring = 64
     max_n = 262144
     outs = [{"hit": torch.empty(max_n, dtype=torch.uint8).pin_memory().numpy(),
@@ -803,127 +809,96 @@ def measure_serve(args, world, local, half_runs: int = 3, half_seconds: float = 
              "material": torch.empty(max_n, dtype=torch.int32).pin_memory().numpy(),
              "voxel": torch.empty((max_n, 3), dtype=torch.int32).pin_memory().numpy(),
              "status": torch.empty(max_n, dtype=torch.uint8).pin_memory().numpy()} for _ in range(ring)]
+    out_ptr = {k: np.array([ptr(o[k]) for o in outs], np.uint64) for k in outs[0]}
     in_place = args.serve_buffers == "in-place"
-    queries = {True: cbq.Query(True, cbq.MAX_FOOTPRINT_DISABLED, True), False: cbq.Query()}
-    server = None
 
-    def submit(k, r):
-        (co, cd), (vo, vd) = pools[r.volume]
-        o, d = (co, cd) if r.collision else (vo, vd)
-        out = {f: v[: r.count] for f, v in outs[k % ring].items()}
-        t, _ = server.submit(dags[r.volume], o[r.start:r.start + r.count], d[r.start:r.start + r.count],
-                             queries[r.collision], out=out)
+    def trace(first: int, count: int) -> np.ndarray:
+        """Requests first .. first + count - 1 of the stream; request k writes ring buffer k % ring."""
+        k = np.arange(count)
+        i = (first + k) % len(reqs)
+        vol, coll = r_vol[i], r_coll[i]
+        t = np.zeros(count, cbq.REQUEST_DTYPE)
+        t["dag"] = dag_h[vol]
+        t["origin_tmax"] = np.where(coll, o_ptr[True][vol], o_ptr[False][vol]) + r_start[i] * np.uint64(16)
+        t["direction"] = np.where(coll, d_ptr[True][vol], d_ptr[False][vol]) + r_start[i] * np.uint64(16)
+        t["ray_count"] = r_count[i]
+        t["compute_surface"] = 1
+        t["max_footprint"] = cbq.MAX_FOOTPRINT_DISABLED
+        t["flags"] = np.where(coll, cbq.QUERY_TMAX, 0)
+        for f, p in out_ptr.items():
+            t[f] = p[(first + k) % ring]
         return t
-
-    # Peak: closed loop with up to `ring` requests outstanding for a fixed count.
-    def closed_loop(first, count):
-        pending = []
-        t0 = time.perf_counter()
-        for k in range(first, first + count):
-            if len(pending) >= ring:
-                server.wait(pending.pop(0))
-            pending.append(submit(k, reqs[k % len(reqs)]))
-        for t in pending:
-            server.wait(t)
-        return time.perf_counter() - t0
 
     def make_server(place):
         return cbq.Server(device_memory_budget=2 << 30, max_inflight_launches=args.serve_inflight,
                           max_batch_requests=128, max_batch_rays=args.serve_batch_rays, in_place=place)
 
-    n_peak = 3000
+    def closed_loop(server, first, count):
+        server.reset_stats()
+        r = server.replay(trace(first, count), np.zeros(count), ring)
+        st = server.stats()
+        return {"requests_per_s": count / r["wall_seconds"], "mrays_per_s": st["rays_completed"] / r["wall_seconds"] / 1e6,
+                "p50_ms": st["latency_p50_us"] / 1e3, "p99_ms": st["latency_p99_us"] / 1e3,
+                "direct_requests": st["direct_requests"], "failed": r["failed"]}
+
+    n_peak = 6000
     other = None
     if sweep:  # the same closed loop through a server of the other buffer mode
         server = make_server(not in_place)
-        closed_loop(0, 300)
-        server.reset_stats()
-        dt_other = closed_loop(300, n_peak)
-        st = server.stats()
-        other = {"buffers": "staged" if in_place else "in-place", "requests_per_s": n_peak / dt_other,
-                 "mrays_per_s": st["rays_completed"] / dt_other / 1e6, "p50_ms": st["latency_p50_us"] / 1e3,
-                 "p99_ms": st["latency_p99_us"] / 1e3}
+        closed_loop(server, 0, 600)
+        other = dict(closed_loop(server, 600, n_peak), buffers="staged" if in_place else "in-place")
         server.close()
     server = make_server(in_place)
-    closed_loop(0, 300)  # warm-up
-    server.reset_stats()
-    dt = closed_loop(300, n_peak)
-    peak = server.stats()
-    peak_rps = n_peak / dt
-    peak_mrays = peak["rays_completed"] / dt / 1e6
+    closed_loop(server, 0, 600)  # warm-up
+    peak = closed_loop(server, 600, n_peak)
+    peak_rps = peak["requests_per_s"]
 
     def open_loop(rate, duration, first):
         """Poisson arrivals at `rate` requests/s for `duration` seconds."""
-        rng = random.Random(rate * 1000.0 + first)
-        times, t = [], 0.0
-        while t < duration:
-            t += rng.expovariate(rate)
-            times.append(t)
-        tickets = [None] * len(times)
-        late = np.zeros(len(times))
-        done = threading.Semaphore(ring)
-
-        def waiter():
-            for i in range(len(times)):
-                while tickets[i] is None:
-                    time.sleep(0)
-                server.wait(tickets[i])
-                done.release()
-
+        rng = np.random.default_rng(int(rate * 1000.0) + first)
+        gaps = rng.exponential(1.0 / rate, size=int(rate * duration * 1.2) + 16)
+        times = np.cumsum(gaps)
+        times = times[times < duration]
         server.reset_stats()
-        th = threading.Thread(target=waiter)
-        th.start()
-        backpressure = 0
-        t0 = time.perf_counter()
-        for i, at in enumerate(times):
-            while time.perf_counter() - t0 < at:
-                pass
-            if not done.acquire(blocking=False):
-                backpressure += 1
-                done.acquire()
-            late[i] = time.perf_counter() - t0 - at
-            tickets[i] = submit(first + i, reqs[(first + i) % len(reqs)])
-        th.join()
-        wall = time.perf_counter() - t0
+        r = server.replay(trace(first, times.size), times, ring)
         st = server.stats()
-        return {"rate_rps": rate, "requests": len(times), "p50_ms": st["latency_p50_us"] / 1e3,
+        late = r["lateness_us"]
+        return {"rate_rps": rate, "requests": int(times.size), "p50_ms": st["latency_p50_us"] / 1e3,
                 "p99_ms": st["latency_p99_us"] / 1e3, "max_ms": st["latency_max_us"] / 1e3,
-                "mrays_per_s": st["rays_completed"] / wall / 1e6, "requests_per_launch": st["mean_requests_per_launch"],
-                "generator_backpressure": backpressure, "direct_requests": st["direct_requests"],
-                "launches": st["launches"],
-                "generator_lateness_ms": {"p50": float(np.quantile(late, 0.5)) * 1e3,
-                                          "p99": float(np.quantile(late, 0.99)) * 1e3,
-                                          "max": float(late.max()) * 1e3}}
+                "mrays_per_s": st["rays_completed"] / r["wall_seconds"] / 1e6,
+                "requests_per_launch": st["mean_requests_per_launch"], "launches": st["launches"],
+                "direct_requests": st["direct_requests"], "failed": r["failed"],
+                "generator_backpressure": r["backpressure"],
+                "generator_lateness_ms": {"p50": float(np.quantile(late, 0.5)) / 1e3,
+                                          "p99": float(np.quantile(late, 0.99)) / 1e3,
+                                          "max": float(late.max()) / 1e3}}
 
     clocks = ClockSampler(local)
     clocks.start()
     # `half_runs` runs at half load; the result is the run with the median p99
     # (host jitter from other work on the machine moves single-run tails).
-    import gc
-    gc.collect()
-    gc.disable()  # no collector pauses in the Python load generator while it runs
     halves = [open_loop(0.5 * peak_rps, half_seconds, 5000 + 40000 * k) for k in range(half_runs)]
     clk = clocks.stop()
     half = dict(sorted(halves, key=lambda r: r["p99_ms"])[len(halves) // 2])
     half["p99_ms_runs"] = [r["p99_ms"] for r in halves]
     sweep_runs = [open_loop(f * peak_rps, 2.0, 9000 + int(f * 1000)) for f in (0.25, 0.75)] if sweep else []
-    gc.enable()
     server.close()
     for g in dags:
         g.destroy()
-    sys.setswitchinterval(old_interval)
     buffers = "page-locked host, served in place" if in_place else "page-locked host, staged through device memory"
     summary = {
         "workload": "serve-8", "edges": [1 << s.edge_log2 for s in scenes],
-        "peak_requests_per_s": peak_rps, "peak_mrays_per_s": peak_mrays,
+        "peak_requests_per_s": peak_rps, "peak_mrays_per_s": peak["mrays_per_s"],
         "half_load": {"rate_rps": half["rate_rps"], "p50_ms": half["p50_ms"], "p99_ms": half["p99_ms"],
                       "p99_ms_runs": half["p99_ms_runs"], "seconds_per_run": half_seconds,
                       "mrays_per_s": half["mrays_per_s"], "requests_per_launch": half["requests_per_launch"],
                       "generator_lateness_ms": half["generator_lateness_ms"]},
         "latency": "submit -> hits in host memory, timed by the server; p99 = median over the runs",
-        "arrivals": "open-loop Poisson from a Python generator", "buffers": buffers, "clocks": clk,
+        "arrivals": "open-loop Poisson, replayed by the library's native driver (cbq_server_replay)",
+        "buffers": buffers, "clocks": clk,
     }
-    details = {"scenes": scenes, "in_place": in_place, "peak": peak, "peak_rps": peak_rps, "peak_mrays": peak_mrays,
-               "other": other, "half": half, "sweep": sweep_runs, "clk": clk, "buffers": buffers}
+    details = {"scenes": scenes, "in_place": in_place, "peak": peak, "peak_rps": peak_rps, "other": other,
+               "half": half, "sweep": sweep_runs, "clk": clk, "buffers": buffers}
     return summary, details
 
 
@@ -940,9 +915,8 @@ def run_gpu_serve(args, world, rank, local):
                    "server": {"memory_budget_gb": 2, "inflight_launches": args.serve_inflight,
                               "max_batch_requests": 128, "max_batch_rays": args.serve_batch_rays,
                               "buffers": d["buffers"]},
-                   "arrivals": "open-loop Poisson"},
-        "peak": {"requests_per_s": d["peak_rps"], "mrays_per_s": d["peak_mrays"], "p50_ms": peak["latency_p50_us"] / 1e3,
-                 "p99_ms": peak["latency_p99_us"] / 1e3, "direct_requests": peak["direct_requests"]},
+                   "arrivals": "open-loop Poisson (native trace driver, cbq_server_replay)"},
+        "peak": peak,
         "peak_other_buffers": d["other"],
         "half_load": half, "sweep": d["sweep"],
         "e2e": {"value": half["mrays_per_s"], "unit": "Mrays/s", "note": "host rays in, host hits out, per request"},

@@ -585,6 +585,23 @@ _sig("cbq_server_reset_stats", [_P])
 _sig("cbq_server_destroy", [_P])
 
 
+class _ReplayResult(ctypes.Structure):
+    _fields_ = [("wall_seconds", ctypes.c_double), ("submitted", ctypes.c_uint64), ("failed", ctypes.c_uint64),
+                ("backpressure", ctypes.c_uint64), ("lateness_p50_us", ctypes.c_double),
+                ("lateness_p99_us", ctypes.c_double), ("lateness_max_us", ctypes.c_double)]
+
+
+_sig("cbq_server_replay", [_P, _P, _P, _U64, _U32, _P, ctypes.POINTER(_ReplayResult)])
+
+# cbq_request as a numpy record, for building request traces without a Python
+# loop per request (pointers as integers; 0 = NULL).
+REQUEST_DTYPE = np.dtype([("dag", np.uint64), ("origin_tmax", np.uint64), ("direction", np.uint64),
+                          ("ray_count", np.uint64), ("compute_surface", np.int32), ("max_footprint", np.float32),
+                          ("flags", np.uint32), ("reserved", np.uint32)] +
+                         [(k, np.uint64) for k in HIT_FIELDS])
+assert REQUEST_DTYPE.itemsize == ctypes.sizeof(_Request)
+
+
 class Server:
     """Continuous-batching request server over resident DAGs (cbq_server).
 
@@ -634,6 +651,23 @@ class Server:
         done = ctypes.c_int32()
         _check(_lib.cbq_server_poll(self._h, ticket, ctypes.byref(done)), "cbq_server_poll")
         return bool(done.value)
+
+    def replay(self, requests: np.ndarray, arrival_s: np.ndarray, max_outstanding: int) -> dict:
+        """Open-loop replay of a request trace from native threads
+        (cbq_server_replay): requests[k] (a REQUEST_DTYPE record whose buffers
+        the caller keeps alive) is submitted arrival_s[k] seconds after the
+        start.  Returns the driver's result with per-request lateness (us)."""
+        req = np.ascontiguousarray(requests, dtype=REQUEST_DTYPE)
+        arr = np.ascontiguousarray(arrival_s, dtype=np.float64)
+        if req.shape != arr.shape:
+            raise ValueError("one arrival time per request")
+        late = np.zeros(req.shape[0], np.float64)
+        res = _ReplayResult()
+        _check(_lib.cbq_server_replay(self._h, _np_ptr(req), _np_ptr(arr), req.shape[0], max_outstanding,
+                                      _np_ptr(late), ctypes.byref(res)), "cbq_server_replay")
+        out = {name: getattr(res, name) for name, _ in _ReplayResult._fields_}
+        out["lateness_us"] = late
+        return out
 
     def stats(self) -> dict:
         s = _ServerStats()

@@ -18,6 +18,7 @@
 #include "cbq_batch.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -370,6 +371,10 @@ void cbq_server::run_scheduler()
     cv_complete.notify_all();
 }
 
+// Completes launches in whatever order they finish: a short launch that ends
+// before a longer one issued earlier is not held behind it.  While launches
+// are in flight this thread polls their events (and yields between rounds);
+// with none in flight it sleeps on the condition variable.
 void cbq_server::run_completer()
 {
     cudaSetDevice(device);
@@ -377,9 +382,33 @@ void cbq_server::run_completer()
     for (;;) {
         cv_complete.wait(lk, [&] { return !inflight.empty() || (scheduler_done && inline_pending == 0); });
         if (inflight.empty()) break;  // scheduler finished and everything completed
-        const int si = inflight.front();
+        const std::vector<int> watch(inflight.begin(), inflight.end());
         lk.unlock();
-        const bool ok = cudaEventSynchronize(slots[si].done) == cudaSuccess;
+        int si = -1;
+        bool ok = true;
+        for (unsigned spin = 0; si < 0; spin++) {
+            for (int w : watch) {
+                const cudaError_t e = cudaEventQuery(slots[w].done);
+                if (e == cudaErrorNotReady) continue;
+                si = w;
+                ok = e == cudaSuccess;
+                if (!ok) cudaGetLastError();
+                break;
+            }
+            if (si >= 0) break;
+            // Launches issued since `watch` was taken are picked up on the next round.
+            if (spin % 64 == 63) {
+                lk.lock();
+                const bool grown = inflight.size() != watch.size();
+                lk.unlock();
+                if (grown) break;
+            }
+            std::this_thread::yield();
+        }
+        if (si < 0) {  // more launches in flight: watch them too
+            lk.lock();
+            continue;
+        }
         if (ok) {  // hits for pageable buffers: copied now that the launch is done
             bool any = false;
             for (Request* rq : slots[si].reqs) {
@@ -395,7 +424,7 @@ void cbq_server::run_completer()
         }
         const Clock::time_point now = Clock::now();
         lk.lock();
-        inflight.pop_front();
+        inflight.erase(std::find(inflight.begin(), inflight.end(), si));
         for (Request* rq : slots[si].reqs) {
             if (!ok && rq->status == CBQ_OK) rq->status = CBQ_ERR_CUDA;
             latencies_us.push_back(std::chrono::duration<double, std::micro>(now - rq->submitted).count());
@@ -625,6 +654,65 @@ cbq_status cbq_server_destroy(cbq_server* s)
     for (Request* rq : s->queue) delete rq;
     delete s;
     return CBQ_OK;
+}
+
+cbq_status cbq_server_replay(cbq_server* s, const cbq_request* requests, const double* arrival_s, uint64_t count,
+                             uint32_t max_outstanding, double* lateness_us, cbq_replay_result* result)
+{
+    if (!s || (count > 0 && (!requests || !arrival_s)) || max_outstanding == 0) return CBQ_ERR_INVALID_ARGUMENT;
+    for (uint64_t k = 1; k < count; k++)
+        if (!(arrival_s[k] >= arrival_s[k - 1])) return CBQ_ERR_INVALID_ARGUMENT;
+    std::vector<uint64_t> tickets(count, 0);
+    std::vector<double> late(count, 0.0);
+    std::atomic<uint64_t> issued{0}, retired{0}, failed{0};
+    std::atomic<bool> abort{false};
+    // Waits for the requests in submission order; `retired` frees their buffers for reuse.
+    std::thread waiter([&] {
+        for (uint64_t k = 0; k < count; k++) {
+            while (issued.load(std::memory_order_acquire) <= k) {
+                if (abort.load(std::memory_order_acquire)) return;
+                std::this_thread::yield();
+            }
+            if (cbq_server_wait(s, tickets[k], -1) != CBQ_OK) failed.fetch_add(1);
+            retired.store(k + 1, std::memory_order_release);
+        }
+    });
+    uint64_t backpressure = 0;
+    cbq_status st = CBQ_OK;
+    const Clock::time_point t0 = Clock::now();
+    for (uint64_t k = 0; k < count; k++) {
+        if (k >= max_outstanding && retired.load(std::memory_order_acquire) <= k - max_outstanding) {
+            backpressure++;
+            while (retired.load(std::memory_order_acquire) <= k - max_outstanding) std::this_thread::yield();
+        }
+        const Clock::time_point at =
+            t0 + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(arrival_s[k]));
+        // Sleep while the arrival is far off, then spin for the last stretch.
+        for (Clock::time_point now = Clock::now(); now < at; now = Clock::now()) {
+            if (at - now > std::chrono::microseconds(300))
+                std::this_thread::sleep_for(at - now - std::chrono::microseconds(200));
+        }
+        late[k] = std::chrono::duration<double, std::micro>(Clock::now() - at).count();
+        st = cbq_server_submit(s, &requests[k], &tickets[k]);
+        if (st != CBQ_OK) break;
+        issued.store(k + 1, std::memory_order_release);
+    }
+    if (st != CBQ_OK) abort.store(true, std::memory_order_release);
+    waiter.join();
+    const double wall = std::chrono::duration<double>(Clock::now() - t0).count();
+    if (lateness_us)
+        for (uint64_t k = 0; k < count; k++) lateness_us[k] = late[k];
+    if (result) {
+        std::memset(result, 0, sizeof(*result));
+        result->wall_seconds = wall;
+        result->submitted = issued.load();
+        result->failed = failed.load();
+        result->backpressure = backpressure;
+        result->lateness_p50_us = percentile(late, 0.50);
+        result->lateness_p99_us = percentile(late, 0.99);
+        result->lateness_max_us = late.empty() ? 0.0 : *std::max_element(late.begin(), late.end());
+    }
+    return st;
 }
 
 }  // extern "C"

@@ -359,8 +359,9 @@ typedef struct cbq_server_stats {
 
 /* Continuous batching: requests are admitted in arrival order while the memory
  * budget and a launch slot allow, grouped into one persistent multi-volume
- * launch per group, and launched while earlier groups still run.  Each result
- * equals cbq_intersect_host on that request alone. */
+ * launch per group, and launched while earlier groups still run; launches are
+ * completed in the order they finish.  Each result equals cbq_intersect_host
+ * on that request alone. */
 typedef struct cbq_server cbq_server;
 
 cbq_status cbq_server_create(const cbq_server_config* cfg, cbq_server** out);
@@ -381,6 +382,26 @@ cbq_status cbq_server_get_stats(cbq_server* s, cbq_server_stats* out);
 cbq_status cbq_server_reset_stats(cbq_server* s);
 /* Finishes every queued and running request, then stops. */
 cbq_status cbq_server_destroy(cbq_server* s);
+
+/* Open-loop load driver (no reference counterpart): replays a request trace
+ * against the server from native threads, so that a serving measurement is
+ * not shaped by the client.  The calling thread submits requests[k] at
+ * arrival_s[k] seconds (non-decreasing) after the call starts, sleeping while
+ * an arrival is far off and spinning for the last 200 us; a second thread
+ * waits for the tickets in order.  Requests k and k + max_outstanding may
+ * share host buffers: request k is submitted only once request
+ * k - max_outstanding has completed (counted in `backpressure`).  Latency per
+ * request is the server's own (cbq_server_get_stats); lateness_us[k]
+ * (optional, count entries) receives how late request k was submitted against
+ * its arrival time.  Returns when every submitted request has completed, or
+ * the first submission error. */
+typedef struct cbq_replay_result {
+    double wall_seconds;            /* call start -> last completion */
+    uint64_t submitted, failed, backpressure;
+    double lateness_p50_us, lateness_p99_us, lateness_max_us;
+} cbq_replay_result;
+cbq_status cbq_server_replay(cbq_server* s, const cbq_request* requests, const double* arrival_s, uint64_t count,
+                             uint32_t max_outstanding, double* lateness_us, cbq_replay_result* result);
 
 /* ------------------------------------------------------- pathtracer */
 

@@ -210,3 +210,49 @@ def test_page_locked_requests_are_served_in_place(served):
     assert direct.stats()["direct_requests"] == len(cases)
     direct.close()
     staged.close()
+
+
+def test_native_replay_of_a_request_trace(served):
+    """cbq_server_replay submits a trace at its arrival times from native
+    threads; with a buffer ring smaller than the trace, a request reuses the
+    buffers of the one `ring` places earlier only after it has completed, so
+    every request's hits can be checked as they land (here each ring slot is
+    checked after the replay against the last request that used it)."""
+    dags, pools = served
+    reqs = W.serve_requests(120, (40000, 128 * 128), seed=11, rays=(1, 9000), volumes=len(dags))
+    ring = 16
+    outs = [cbq.alloc_host_hits(9000) for _ in range(ring)]
+    trace = np.zeros(len(reqs), cbq.REQUEST_DTYPE)
+    keep = []
+    for k, r in enumerate(reqs):
+        (co, cd), (vo, vd) = pools[r.volume]
+        o, d = (co, cd) if r.collision else (vo, vd)
+        o, d = np.ascontiguousarray(o[r.start:r.start + r.count]), np.ascontiguousarray(d[r.start:r.start + r.count])
+        keep.append((o, d))
+        trace[k]["dag"] = dags[r.volume].handle.value
+        trace[k]["origin_tmax"] = o.ctypes.data
+        trace[k]["direction"] = d.ctypes.data
+        trace[k]["ray_count"] = r.count
+        trace[k]["compute_surface"] = 1
+        trace[k]["max_footprint"] = cbq.MAX_FOOTPRINT_DISABLED
+        trace[k]["flags"] = cbq.QUERY_TMAX if r.collision else 0
+        for f in cbq.HIT_FIELDS:
+            trace[k][f] = outs[k % ring][f].ctypes.data
+    arrivals = np.cumsum(np.full(len(reqs), 2e-4))  # 5k requests/s
+    server = cbq.Server(device_memory_budget=64 << 20, max_inflight_launches=3, max_batch_requests=16)
+    res = server.replay(trace, arrivals, ring)
+    assert res["submitted"] == len(reqs) and res["failed"] == 0
+    assert res["wall_seconds"] >= arrivals[-1]
+    assert res["lateness_us"].shape == (len(reqs),) and (res["lateness_us"] >= 0).all()
+    st = server.stats()
+    assert st["completed"] == len(reqs) and st["latency_p99_us"] > 0
+    for slot in range(ring):
+        k = max(k for k in range(len(reqs)) if k % ring == slot)
+        r = reqs[k]
+        o, d = keep[k]
+        want = cbq.intersect_volume_host(dags[r.volume], o, d, use_tmax=r.collision)
+        _same({f: v[: r.count] for f, v in outs[slot].items()}, want)
+    # Arrival times must not decrease.
+    with pytest.raises(cbq.CbqError):
+        server.replay(trace[:2], np.array([1e-3, 0.0]), ring)
+    server.close()
