@@ -159,6 +159,13 @@ class _Job(ctypes.Structure):
 _sig("cbq_batch_create", [ctypes.POINTER(_Job), ctypes.c_int32, ctypes.POINTER(_Query), ctypes.POINTER(_P)])
 _sig("cbq_batch_set_config", [_P, ctypes.c_int32, _U32])
 _sig("cbq_batch_get_config", [_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(_U32), ctypes.POINTER(_U64)])
+class _BatchConfig(ctypes.Structure):
+    _fields_ = [("block", ctypes.c_int32), ("refill_min", ctypes.c_uint32), ("steps", ctypes.c_int32),
+                ("registers", ctypes.c_int32), ("stack", ctypes.c_int32), ("form", ctypes.c_int32)]
+
+
+_sig("cbq_batch_set_launch_config", [_P, ctypes.POINTER(_BatchConfig)])
+_sig("cbq_batch_get_launch_config", [_P, ctypes.POINTER(_BatchConfig)])
 _sig("cbq_batch_autotune", [_P, _P, ctypes.c_int32])
 _sig("cbq_batch_launch", [_P, _P])
 _sig("cbq_batch_launch_direct", [_P, _P])
@@ -806,15 +813,23 @@ class Batch:
         return self.config()["total_rays"]
 
     def config(self) -> dict:
-        b = ctypes.c_int32()
-        r = _U32()
+        """The launch configuration (block, refill_min, steps, registers, stack,
+        form) and the batch's ray count."""
         t = _U64()
-        _check(_lib.cbq_batch_get_config(self._h, ctypes.byref(b), ctypes.byref(r), ctypes.byref(t)),
-               "cbq_batch_get_config")
-        return {"block": b.value, "refill_min": r.value, "total_rays": t.value}
+        _check(_lib.cbq_batch_get_config(self._h, None, None, ctypes.byref(t)), "cbq_batch_get_config")
+        c = _BatchConfig()
+        _check(_lib.cbq_batch_get_launch_config(self._h, ctypes.byref(c)), "cbq_batch_get_launch_config")
+        out = {name: getattr(c, name) for name, _ in _BatchConfig._fields_}
+        out["total_rays"] = t.value
+        return out
 
     def set_config(self, block: int = 0, refill_min: int = 0) -> None:
         _check(_lib.cbq_batch_set_config(self._h, block, refill_min), "cbq_batch_set_config")
+
+    def set_launch_config(self, block: int = 128, refill_min: int = 8, steps: int = 8, registers: int = 0,
+                          stack: int = STACK_LOCAL, form: int = FORM_PERSISTENT) -> None:
+        c = _BatchConfig(block, refill_min, steps, registers, stack, form)
+        _check(_lib.cbq_batch_set_launch_config(self._h, ctypes.byref(c)), "cbq_batch_set_launch_config")
 
     def autotune(self, repetitions: int = 3, stream=None) -> dict:
         _check(_lib.cbq_batch_autotune(self._h, _stream_ptr(stream), repetitions), "cbq_batch_autotune")

@@ -36,18 +36,35 @@ struct BatchSrc {
 
 constexpr unsigned kFullMask = 0xffffffffu;
 
-// Descent stack in local memory and `steps` ESVO steps per loop iteration:
-// the faster choices for the single-volume kernel on GB300.  Every job of one
-// launch has the node store layout COMPACT.
-template <bool COMPACT>
+// Last job whose first ray is <= g, by binary search over the prefix offsets
+// (prefix[lo] <= g < prefix[hi]; every job in the table has at least one ray).
+__device__ __forceinline__ uint32_t job_of(const uint64_t* prefix, uint32_t njobs, uint64_t g)
+{
+    uint32_t lo = 0, hi = njobs;
+    while (hi - lo > 1u) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (prefix[mid] <= g) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// `steps` ESVO steps per loop iteration.  SHARED: descent stack in shared
+// memory (`stack_rows` rows after the prefix offsets, one column per thread)
+// instead of a per-thread local array.  SORTED: global ray g of the launch is
+// ray perm[g], a ray of the same job (launch_batch_octant_sort).  Every job of
+// one launch has the node store layout COMPACT.
+template <bool COMPACT, bool SHARED, bool SORTED>
 __device__ __forceinline__ void batch_body(const JobDesc* __restrict__ jobs, uint32_t njobs, uint64_t total,
                                            unsigned long long* __restrict__ counter, uint32_t refill_min,
-                                           uint32_t steps)
+                                           uint32_t steps, const uint32_t* __restrict__ perm)
 {
-    extern __shared__ uint64_t prefix[];  // njobs + 1 entries
-    LocalStack stack;
+    extern __shared__ uint64_t prefix[];  // njobs + 1 entries, then the shared stack
     for (uint32_t j = threadIdx.x; j <= njobs; j += blockDim.x) prefix[j] = j < njobs ? jobs[j].first : total;
     __syncthreads();
+    LocalStack lstack;
+    SharedStack sstack;
+    sstack.base = (uint32_t*)(prefix + njobs + 1) + threadIdx.x;
+    sstack.stride = blockDim.x;
 
     BatchSrc<COMPACT> c;
     c.jobs = jobs;
@@ -68,18 +85,13 @@ __device__ __forceinline__ void batch_body(const JobDesc* __restrict__ jobs, uin
                 if ((int)lane == leader) base = atomicAdd(counter, (unsigned long long)cnt);
                 base = __shfl_sync(kFullMask, base, leader);
                 if (L.mode == kLaneIdle) {
-                    const uint64_t g = base + __popc(idle & below);
+                    uint64_t g = base + __popc(idle & below);
                     if (g < total) {
-                        // Last job whose first ray is <= g.  Every job in the
-                        // table has at least one ray.
-                        uint32_t lo = 0, hi = njobs;  // prefix[lo] <= g < prefix[hi]
-                        while (hi - lo > 1u) {
-                            const uint32_t mid = (lo + hi) >> 1;
-                            if (prefix[mid] <= g) lo = mid; else hi = mid;
-                        }
-                        L.job = lo;
-                        L.nodes = jobs[lo].nodes;
-                        lane_begin(L, c, g - prefix[lo]);
+                        if (SORTED) g = __ldg(perm + g);
+                        const uint32_t j = job_of(prefix, njobs, g);
+                        L.job = j;
+                        L.nodes = jobs[j].nodes;
+                        lane_begin(L, c, g - prefix[j]);
                     }
                 }
                 if (base + cnt >= total) more = false;
@@ -90,26 +102,89 @@ __device__ __forceinline__ void batch_body(const JobDesc* __restrict__ jobs, uin
             continue;
         }
         lane_settle(L, c);
-        lane_walk_steps(L, c, stack, steps);
+        if (SHARED)
+            lane_walk_steps(L, c, sstack, steps);
+        else
+            lane_walk_steps(L, c, lstack, steps);
     }
 }
 
-template <bool COMPACT>
+template <bool COMPACT, bool SHARED, bool SORTED>
 __global__ void __launch_bounds__(256) cbq_k_flat_batch(const JobDesc* __restrict__ jobs, uint32_t njobs,
                                                         uint64_t total, unsigned long long* __restrict__ counter,
-                                                        uint32_t refill_min, uint32_t steps)
+                                                        uint32_t refill_min, uint32_t steps,
+                                                        const uint32_t* __restrict__ perm)
 {
-    batch_body<COMPACT>(jobs, njobs, total, counter, refill_min, steps);
+    batch_body<COMPACT, SHARED, SORTED>(jobs, njobs, total, counter, refill_min, steps, perm);
 }
 
-// The same held to 56 registers per thread (more resident warps); a batch
-// autotuner choice like the single-volume kernel's.
-template <bool COMPACT>
+// The local-stack form held to 56 registers per thread (more resident warps);
+// a batch autotuner choice like the single-volume kernel's.
+template <bool COMPACT, bool SORTED>
 __global__ void __maxnreg__(56) cbq_k_flat_batch_r56(const JobDesc* __restrict__ jobs, uint32_t njobs,
                                                      uint64_t total, unsigned long long* __restrict__ counter,
-                                                     uint32_t refill_min, uint32_t steps)
+                                                     uint32_t refill_min, uint32_t steps,
+                                                     const uint32_t* __restrict__ perm)
 {
-    batch_body<COMPACT>(jobs, njobs, total, counter, refill_min, steps);
+    batch_body<COMPACT, false, SORTED>(jobs, njobs, total, counter, refill_min, steps, perm);
+}
+
+// Octant of a ray: its direction sign bits (raytracing.cpp:416-417).
+__device__ __forceinline__ uint32_t batch_octant(float4 d)
+{
+    return (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+}
+
+// counts[8 * job + octant] += rays, warp-aggregated.
+__global__ void __launch_bounds__(256) cbq_k_batch_octant_count(const JobDesc* __restrict__ jobs, uint32_t njobs,
+                                                                uint64_t total, uint32_t* __restrict__ counts)
+{
+    extern __shared__ uint64_t prefix[];
+    for (uint32_t j = threadIdx.x; j <= njobs; j += blockDim.x) prefix[j] = j < njobs ? jobs[j].first : total;
+    __syncthreads();
+    const unsigned lane = threadIdx.x & 31u;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t g0 = (uint64_t)blockIdx.x * blockDim.x; g0 < total; g0 += stride) {
+        const uint64_t g = g0 + threadIdx.x;
+        const bool valid = g < total;
+        const unsigned act = __ballot_sync(kFullMask, valid);
+        if (!valid) continue;
+        const uint32_t j = job_of(prefix, njobs, g);
+        const uint32_t key = 8u * j + batch_octant(__ldg(jobs[j].dir + (g - prefix[j])));
+        const unsigned grp = __match_any_sync(act, key);
+        if ((int)lane == __ffs(grp) - 1) atomicAdd(&counts[key], (uint32_t)__popc(grp));
+    }
+}
+
+// perm[first(job) + (rays of lower octants in the job) + k] = g.  Every global
+// index g < total is written exactly once, inside its own job's range.
+__global__ void __launch_bounds__(256) cbq_k_batch_octant_scatter(const JobDesc* __restrict__ jobs, uint32_t njobs,
+                                                                  uint64_t total, const uint32_t* __restrict__ counts,
+                                                                  uint32_t* __restrict__ cursor,
+                                                                  uint32_t* __restrict__ perm)
+{
+    extern __shared__ uint64_t prefix[];
+    for (uint32_t j = threadIdx.x; j <= njobs; j += blockDim.x) prefix[j] = j < njobs ? jobs[j].first : total;
+    __syncthreads();
+    const unsigned lane = threadIdx.x & 31u;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t g0 = (uint64_t)blockIdx.x * blockDim.x; g0 < total; g0 += stride) {
+        const uint64_t g = g0 + threadIdx.x;
+        const bool valid = g < total;
+        const unsigned act = __ballot_sync(kFullMask, valid);
+        if (!valid) continue;
+        const uint32_t j = job_of(prefix, njobs, g);
+        const uint32_t oct = batch_octant(__ldg(jobs[j].dir + (g - prefix[j])));
+        const uint32_t key = 8u * j + oct;
+        const unsigned grp = __match_any_sync(act, key);
+        const int leader = __ffs(grp) - 1;
+        uint32_t base = 0;
+        if ((int)lane == leader) base = atomicAdd(&cursor[key], (uint32_t)__popc(grp));
+        base = __shfl_sync(grp, base, leader);
+        uint64_t start = prefix[j];
+        for (uint32_t o = 0; o < oct; o++) start += counts[8u * j + o];
+        perm[start + base + __popc(grp & ((1u << lane) - 1u))] = (uint32_t)g;
+    }
 }
 
 }  // namespace dev
@@ -130,39 +205,80 @@ void fill_job_volume(dev::JobDesc& d, const cbq_dag* dag)
 
 namespace {
 
-template <bool COMPACT>
-cbq_status launch_batch_layout(const dev::JobDesc* d_jobs, uint32_t njobs, uint64_t total, uint64_t* counter,
-                               int block, uint32_t refill, uint32_t steps, bool registers56, int device,
-                               cudaStream_t s)
+template <bool COMPACT, bool SHARED, bool SORTED>
+cbq_status launch_batch_variant(const dev::JobDesc* d_jobs, uint32_t njobs, uint64_t total, uint64_t* counter,
+                                int device, cudaStream_t s, const BatchLaunch& bl)
 {
-    const auto kernel = registers56 ? dev::cbq_k_flat_batch_r56<COMPACT> : dev::cbq_k_flat_batch<COMPACT>;
+    auto kernel = dev::cbq_k_flat_batch<COMPACT, SHARED, SORTED>;
+    if constexpr (!SHARED) {
+        if (bl.registers56) kernel = dev::cbq_k_flat_batch_r56<COMPACT, SORTED>;
+    }
     if (cudaMemsetAsync(counter, 0, sizeof(uint64_t), s) != cudaSuccess) return CBQ_ERR_CUDA;
-    const size_t smem = (size_t)(njobs + 1) * 8;  // the prefix offsets
+    // The prefix offsets, then (shared stack) one column of stack_rows slots per thread.
+    const size_t smem = (size_t)(njobs + 1) * 8 + (SHARED ? (size_t)std::max(1, bl.stack_rows) * bl.block * 4 : 0);
     if (smem > 227u * 1024u) return CBQ_ERR_CAPACITY;
     if (smem > 48u * 1024u &&
         cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return CBQ_ERR_CUDA;
     int sms = 0, per_sm = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return CBQ_ERR_CUDA;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, bl.block, smem) != cudaSuccess)
         return CBQ_ERR_CUDA;
     per_sm = std::max(per_sm, 1);
-    kernel<<<sms * per_sm, block, smem, s>>>(d_jobs, njobs, total, (unsigned long long*)counter, refill, steps);
+    kernel<<<sms * per_sm, bl.block, smem, s>>>(d_jobs, njobs, total, (unsigned long long*)counter, bl.refill,
+                                                bl.steps ? bl.steps : 1u, bl.perm);
     return cudaGetLastError() == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
+}
+
+template <bool COMPACT>
+cbq_status launch_batch_layout(const dev::JobDesc* d_jobs, uint32_t njobs, uint64_t total, uint64_t* counter,
+                               int device, cudaStream_t s, const BatchLaunch& bl)
+{
+    const bool sorted = bl.perm != nullptr;
+    if (bl.shared_stack)
+        return sorted ? launch_batch_variant<COMPACT, true, true>(d_jobs, njobs, total, counter, device, s, bl)
+                      : launch_batch_variant<COMPACT, true, false>(d_jobs, njobs, total, counter, device, s, bl);
+    return sorted ? launch_batch_variant<COMPACT, false, true>(d_jobs, njobs, total, counter, device, s, bl)
+                  : launch_batch_variant<COMPACT, false, false>(d_jobs, njobs, total, counter, device, s, bl);
 }
 
 }  // namespace
 
 cbq_status launch_batch_kernel(const dev::JobDesc* d_jobs, uint32_t njobs, uint64_t total, uint64_t* counter,
+                               bool compact, int device, cudaStream_t s, const BatchLaunch& bl)
+{
+    if (total == 0 || njobs == 0) return CBQ_OK;
+    return compact ? launch_batch_layout<true>(d_jobs, njobs, total, counter, device, s, bl)
+                   : launch_batch_layout<false>(d_jobs, njobs, total, counter, device, s, bl);
+}
+
+cbq_status launch_batch_kernel(const dev::JobDesc* d_jobs, uint32_t njobs, uint64_t total, uint64_t* counter,
                                int block, uint32_t refill, uint32_t steps, bool compact, int device, cudaStream_t s,
                                bool registers56)
 {
+    BatchLaunch bl;
+    bl.block = block;
+    bl.refill = refill;
+    bl.steps = steps;
+    bl.registers56 = registers56;
+    return launch_batch_kernel(d_jobs, njobs, total, counter, compact, device, s, bl);
+}
+
+cbq_status launch_batch_octant_sort(const dev::JobDesc* d_jobs, uint32_t njobs, uint64_t total, uint32_t* scratch,
+                                    uint32_t* perm, int device, cudaStream_t s)
+{
     if (total == 0 || njobs == 0) return CBQ_OK;
-    if (steps == 0) steps = 1;
-    return compact ? launch_batch_layout<true>(d_jobs, njobs, total, counter, block, refill, steps, registers56,
-                                               device, s)
-                   : launch_batch_layout<false>(d_jobs, njobs, total, counter, block, refill, steps, registers56,
-                                                device, s);
+    if (total > 0xffffffffull) return CBQ_ERR_INVALID_ARGUMENT;  // perm holds 32-bit ray indices
+    const size_t smem = (size_t)(njobs + 1) * 8;
+    if (smem > 48u * 1024u) return CBQ_ERR_CAPACITY;
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return CBQ_ERR_CUDA;
+    if (cudaMemsetAsync(scratch, 0, (size_t)njobs * 16 * sizeof(uint32_t), s) != cudaSuccess) return CBQ_ERR_CUDA;
+    const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((total + 255) / 256, (uint64_t)sms * 8));
+    dev::cbq_k_batch_octant_count<<<grid, 256, smem, s>>>(d_jobs, njobs, total, scratch);
+    dev::cbq_k_batch_octant_scatter<<<grid, 256, smem, s>>>(d_jobs, njobs, total, scratch, scratch + 8 * njobs,
+                                                            perm);
+    return cudaGetLastError() == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
 }
 
 }  // namespace cbq
@@ -183,16 +299,45 @@ struct cbq_batch {
     uint32_t njobs_ref = 0;                 // of which reference layout (one launch per layout)
     uint64_t total = 0;
     uint64_t total_ref = 0;
-    uint32_t steps = kBatchStepsDefault;
-    bool registers56 = false;
+    int stack_rows = 1;                     // max SubDAG height over the jobs
     uint64_t* d_counter = nullptr;
+    uint32_t* d_sort = nullptr;             // octant order: 16 uint32 per job, then one index per ray
     cbq_query query{1, CBQ_MAX_FOOTPRINT_DISABLED, 0u, 0u};
-    int block = kBatchBlockDefault;
-    uint32_t refill = kBatchRefillDefault;
+    cbq_batch_config cfg{kBatchBlockDefault, kBatchRefillDefault, (int32_t)kBatchStepsDefault, 0, CBQ_STACK_LOCAL,
+                         CBQ_FORM_PERSISTENT};
     cudaGraphExec_t exec = nullptr;
 };
 
 namespace {
+
+BatchLaunch batch_launch(const cbq_batch* b, const uint32_t* perm)
+{
+    BatchLaunch bl;
+    bl.block = b->cfg.block;
+    bl.refill = b->cfg.refill_min;
+    bl.steps = (uint32_t)b->cfg.steps;
+    bl.registers56 = b->cfg.registers == 56 && b->cfg.stack == CBQ_STACK_LOCAL;
+    bl.shared_stack = b->cfg.stack == CBQ_STACK_SHARED;
+    bl.stack_rows = b->stack_rows;
+    bl.perm = perm;
+    return bl;
+}
+
+// Device memory of the octant order, allocated when a sorted form is first
+// chosen.  The sort keeps a job's first ray index per job in shared memory and
+// writes 32-bit ray indices, which bounds the jobs and rays of a sorted batch.
+cbq_status ensure_sort_scratch(cbq_batch* b)
+{
+    if ((size_t)(b->njobs + 1) * 8 > 48u * 1024u || b->total > 0xffffffffull) return CBQ_ERR_CAPACITY;
+    if (b->d_sort || b->njobs == 0) return CBQ_OK;
+    const size_t bytes = ((size_t)b->njobs * 16 + b->total) * sizeof(uint32_t);
+    if (cudaMalloc((void**)&b->d_sort, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        b->d_sort = nullptr;
+        return CBQ_ERR_OUT_OF_MEMORY;
+    }
+    return CBQ_OK;
+}
 
 cbq_status enqueue_batch(cbq_batch* b, cudaStream_t s)
 {
@@ -201,11 +346,26 @@ cbq_status enqueue_batch(cbq_batch* b, cudaStream_t s)
         cbq_status st = cbq_intersect(jb.dag, &jb.rays, jb.ray_count, &b->query, &jb.hits, (cbq_stream_t)s);
         if (st != CBQ_OK) return st;
     }
-    cbq_status st = launch_batch_kernel(b->d_jobs, b->njobs_ref, b->total_ref, b->d_counter, b->block, b->refill,
-                                        b->steps, false, b->device, s, b->registers56);
+    // One launch per node store layout, each with its own ray index space.
+    const uint32_t njobs_c = b->njobs - b->njobs_ref;
+    const uint64_t total_c = b->total - b->total_ref;
+    const bool sorted = b->cfg.form == CBQ_FORM_SORTED;
+    if (sorted && !b->d_sort) return CBQ_ERR_INVALID_ARGUMENT;
+    uint32_t* perm_ref = sorted ? b->d_sort + 16 * (size_t)b->njobs : nullptr;
+    uint32_t* perm_c = sorted ? perm_ref + b->total_ref : nullptr;
+    if (sorted) {
+        cbq_status st = launch_batch_octant_sort(b->d_jobs, b->njobs_ref, b->total_ref, b->d_sort, perm_ref,
+                                                 b->device, s);
+        if (st == CBQ_OK)
+            st = launch_batch_octant_sort(b->d_jobs + b->njobs_ref, njobs_c, total_c, b->d_sort + 16 * b->njobs_ref,
+                                          perm_c, b->device, s);
+        if (st != CBQ_OK) return st;
+    }
+    cbq_status st = launch_batch_kernel(b->d_jobs, b->njobs_ref, b->total_ref, b->d_counter, false, b->device, s,
+                                        batch_launch(b, perm_ref));
     if (st != CBQ_OK) return st;
-    return launch_batch_kernel(b->d_jobs + b->njobs_ref, b->njobs - b->njobs_ref, b->total - b->total_ref,
-                               b->d_counter + 8, b->block, b->refill, b->steps, true, b->device, s, b->registers56);
+    return launch_batch_kernel(b->d_jobs + b->njobs_ref, njobs_c, total_c, b->d_counter + 8, true, b->device, s,
+                               batch_launch(b, perm_c));
 }
 
 void drop_graph(cbq_batch* b)
@@ -236,6 +396,16 @@ cbq_status capture_graph(cbq_batch* b)
     return st;
 }
 
+cbq_status check_config(const cbq_batch_config& c)
+{
+    if (c.block < 32 || c.block > 256 || (c.block % 32) != 0) return CBQ_ERR_INVALID_ARGUMENT;
+    if (c.refill_min < 1 || c.refill_min > 32 || c.steps < 1 || c.steps > 16) return CBQ_ERR_INVALID_ARGUMENT;
+    if (c.registers != 0 && c.registers != 56) return CBQ_ERR_INVALID_ARGUMENT;
+    if (c.stack != CBQ_STACK_LOCAL && c.stack != CBQ_STACK_SHARED) return CBQ_ERR_INVALID_ARGUMENT;
+    if (c.form != CBQ_FORM_PERSISTENT && c.form != CBQ_FORM_SORTED) return CBQ_ERR_INVALID_ARGUMENT;
+    return CBQ_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -264,6 +434,7 @@ cbq_status cbq_batch_create(const cbq_job* jobs, int32_t job_count, const cbq_qu
         b->jobs.push_back(jb);
         if (jb.ray_count == 0) continue;
         if (!jb.dag->flat_ok) { b->nested_jobs.push_back(j); continue; }
+        b->stack_rows = std::max(b->stack_rows, (int)jb.dag->max_height);
         dev::JobDesc d;
         std::memset(&d, 0, sizeof(d));
         fill_job_volume(d, jb.dag);
@@ -309,8 +480,8 @@ cbq_status cbq_batch_create(const cbq_job* jobs, int32_t job_count, const cbq_qu
 cbq_status cbq_batch_set_config(cbq_batch* b, int32_t block, uint32_t refill_min)
 {
     if (!b || block < 0 || block > 256 || (block % 32) != 0 || refill_min > 32) return CBQ_ERR_INVALID_ARGUMENT;
-    b->block = block ? block : kBatchBlockDefault;
-    b->refill = refill_min ? refill_min : kBatchRefillDefault;
+    b->cfg.block = block ? block : kBatchBlockDefault;
+    b->cfg.refill_min = refill_min ? refill_min : kBatchRefillDefault;
     drop_graph(b);
     return CBQ_OK;
 }
@@ -318,9 +489,27 @@ cbq_status cbq_batch_set_config(cbq_batch* b, int32_t block, uint32_t refill_min
 cbq_status cbq_batch_get_config(const cbq_batch* b, int32_t* block, uint32_t* refill_min, uint64_t* total_rays)
 {
     if (!b) return CBQ_ERR_INVALID_ARGUMENT;
-    if (block) *block = b->block;
-    if (refill_min) *refill_min = b->refill;
+    if (block) *block = b->cfg.block;
+    if (refill_min) *refill_min = b->cfg.refill_min;
     if (total_rays) *total_rays = b->total;
+    return CBQ_OK;
+}
+
+cbq_status cbq_batch_set_launch_config(cbq_batch* b, const cbq_batch_config* cfg)
+{
+    if (!b || !cfg) return CBQ_ERR_INVALID_ARGUMENT;
+    cbq_status st = check_config(*cfg);
+    if (st != CBQ_OK) return st;
+    if (cfg->form == CBQ_FORM_SORTED && (st = ensure_sort_scratch(b)) != CBQ_OK) return st;
+    b->cfg = *cfg;
+    drop_graph(b);
+    return CBQ_OK;
+}
+
+cbq_status cbq_batch_get_launch_config(const cbq_batch* b, cbq_batch_config* cfg)
+{
+    if (!b || !cfg) return CBQ_ERR_INVALID_ARGUMENT;
+    *cfg = b->cfg;
     return CBQ_OK;
 }
 
@@ -345,48 +534,58 @@ cbq_status cbq_batch_autotune(cbq_batch* b, cbq_stream_t stream, int32_t repetit
     if (!b || repetitions <= 0) return CBQ_ERR_INVALID_ARGUMENT;
     static const int blocks[] = {64, 128, 256};
     static const uint32_t refills[] = {4, 8, 12, 16};
-    static const uint32_t step_counts[] = {4, 8, 16};
+    static const int32_t step_counts[] = {4, 8, 16};
+    // Kernel variants: local stack (64 registers), local stack held to 56
+    // registers, shared-memory stack; each with the rays in the order given or
+    // grouped by octant per job.
+    struct Variant { int32_t registers, stack, form; };
+    static const Variant variants[] = {
+        {0, CBQ_STACK_LOCAL, CBQ_FORM_PERSISTENT}, {56, CBQ_STACK_LOCAL, CBQ_FORM_PERSISTENT},
+        {0, CBQ_STACK_SHARED, CBQ_FORM_PERSISTENT}, {0, CBQ_STACK_LOCAL, CBQ_FORM_SORTED},
+        {56, CBQ_STACK_LOCAL, CBQ_FORM_SORTED}, {0, CBQ_STACK_SHARED, CBQ_FORM_SORTED}};
+    const bool can_sort = ensure_sort_scratch(b) == CBQ_OK;  // without the scratch, unsorted forms only
     cudaEvent_t e0, e1;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return CBQ_ERR_CUDA;
+    const cbq_batch_config saved = b->cfg;
+    cbq_batch_config best_cfg = saved;
     float best = 1e30f;
-    int best_block = b->block;
-    uint32_t best_refill = b->refill, best_steps = b->steps;
-    bool best_r56 = b->registers56;
     cbq_status st = CBQ_OK;
-    for (int k = 0; k < 3 * 4 * 3 * 2 && st == CBQ_OK; k++) {
-        const int blk = blocks[k / 24];
-        const uint32_t rf = refills[(k / 6) % 4];
-        b->block = blk;
-        b->refill = rf;
-        b->steps = step_counts[(k / 2) % 3];
-        b->registers56 = (k & 1) != 0;
-        st = enqueue_batch(b, (cudaStream_t)stream);  // warm-up
-        if (st != CBQ_OK) break;
-        cudaEventRecord(e0, (cudaStream_t)stream);
-        for (int r = 0; r < repetitions && st == CBQ_OK; r++) st = enqueue_batch(b, (cudaStream_t)stream);
-        cudaEventRecord(e1, (cudaStream_t)stream);
-        if (st != CBQ_OK || cudaEventSynchronize(e1) != cudaSuccess) { st = CBQ_ERR_CUDA; break; }
-        float ms = 0;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (ms < best) {
-            best = ms;
-            best_block = blk;
-            best_refill = rf;
-            best_steps = b->steps;
-            best_r56 = b->registers56;
+    for (int blk : blocks) {
+        for (uint32_t rf : refills) {
+            for (int32_t steps : step_counts) {
+                for (const Variant& v : variants) {
+                    if (v.form == CBQ_FORM_SORTED && !can_sort) continue;
+                    b->cfg = cbq_batch_config{blk, rf, steps, v.registers, v.stack, v.form};
+                    st = enqueue_batch(b, (cudaStream_t)stream);  // warm-up
+                    if (st != CBQ_OK) break;
+                    cudaEventRecord(e0, (cudaStream_t)stream);
+                    for (int r = 0; r < repetitions && st == CBQ_OK; r++) st = enqueue_batch(b, (cudaStream_t)stream);
+                    cudaEventRecord(e1, (cudaStream_t)stream);
+                    if (st != CBQ_OK || cudaEventSynchronize(e1) != cudaSuccess) { st = CBQ_ERR_CUDA; break; }
+                    float ms = 0;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    if (ms < best) {
+                        best = ms;
+                        best_cfg = b->cfg;
+                    }
+                }
+                if (st != CBQ_OK) break;
+            }
+            if (st != CBQ_OK) break;
         }
+        if (st != CBQ_OK) break;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    b->block = best_block;
-    b->refill = best_refill;
-    b->steps = best_steps;
-    b->registers56 = best_r56;
+    b->cfg = st == CBQ_OK ? best_cfg : saved;
     drop_graph(b);
     if (st == CBQ_OK)
         cbq::log(CBQ_LOG_INFO,
-                 "batch autotune: block %d, refill %u, %u steps per iteration, %d registers: %.3f ms per launch",
-                 best_block, best_refill, best_steps, best_r56 ? 56 : 64, best / (float)repetitions);
+                 "batch autotune: block %d, refill %u, %d steps per iteration, %d registers, %s stack, %s: "
+                 "%.3f ms per launch",
+                 best_cfg.block, best_cfg.refill_min, best_cfg.steps, best_cfg.registers ? 56 : 64,
+                 best_cfg.stack == CBQ_STACK_SHARED ? "shared" : "local",
+                 best_cfg.form == CBQ_FORM_SORTED ? "octant-sorted" : "rays as given", best / (float)repetitions);
     return st;
 }
 
@@ -395,6 +594,7 @@ cbq_status cbq_batch_destroy(cbq_batch* b)
     if (!b) return CBQ_ERR_INVALID_ARGUMENT;
     drop_graph(b);
     if (b->d_counter) cudaFree(b->d_counter);
+    if (b->d_sort) cudaFree(b->d_sort);
     delete b;
     return CBQ_OK;
 }

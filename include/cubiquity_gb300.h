@@ -301,8 +301,25 @@ cbq_status cbq_batch_create(const cbq_job* jobs, int32_t job_count, const cbq_qu
  * trigger a warp's refill (1..32, 0 = default).  Re-captures on next launch. */
 cbq_status cbq_batch_set_config(cbq_batch* b, int32_t block, uint32_t refill_min);
 cbq_status cbq_batch_get_config(const cbq_batch* b, int32_t* block, uint32_t* refill_min, uint64_t* total_rays);
-/* Times the candidate launch shapes on this batch (synchronous) and keeps the
- * fastest. */
+
+/* The batch's full launch configuration.  Every choice gives the same results. */
+typedef struct cbq_batch_config {
+    int32_t block;            /* threads per block: 32..256, a multiple of 32 */
+    uint32_t refill_min;      /* idle lanes that trigger a warp's refill: 1..32 */
+    int32_t steps;            /* ESVO steps per loop iteration: 1..16 */
+    int32_t registers;        /* 0, or 56: the local-stack kernel held to 56 registers */
+    int32_t stack;            /* CBQ_STACK_LOCAL or CBQ_STACK_SHARED (descent stack placement) */
+    int32_t form;             /* CBQ_FORM_PERSISTENT: rays in the order given; CBQ_FORM_SORTED: each
+                                 job's rays grouped by octant first (two small kernels per launch;
+                                 4 bytes of device memory per ray, allocated when first chosen) */
+} cbq_batch_config;
+cbq_status cbq_batch_set_launch_config(cbq_batch* b, const cbq_batch_config* cfg);
+cbq_status cbq_batch_get_launch_config(const cbq_batch* b, cbq_batch_config* cfg);
+
+/* Autotuner of the batched form: times block {64,128,256} x refill
+ * {4,8,12,16} x steps {4,8,16} x {local stack, local stack at 56 registers,
+ * shared-memory stack} x {rays as given, octant-sorted} on this batch
+ * (synchronous; `repetitions` launches each) and keeps the fastest. */
 cbq_status cbq_batch_autotune(cbq_batch* b, cbq_stream_t stream, int32_t repetitions);
 /* Replays the captured graph on `stream` (captures it first if needed). */
 cbq_status cbq_batch_launch(cbq_batch* b, cbq_stream_t stream);

@@ -85,12 +85,50 @@ def test_batch_launch_shapes_do_not_change_results(small_batch, block, refill):
     batch.destroy()
 
 
+@pytest.mark.parametrize("registers,stack,form", [(0, cbq.STACK_LOCAL, cbq.FORM_SORTED),
+                                                  (56, cbq.STACK_LOCAL, cbq.FORM_SORTED),
+                                                  (0, cbq.STACK_SHARED, cbq.FORM_PERSISTENT),
+                                                  (0, cbq.STACK_SHARED, cbq.FORM_SORTED)])
+@pytest.mark.parametrize("block,steps", [(64, 4), (256, 16)])
+def test_batch_stack_and_octant_order_do_not_change_results(small_batch, registers, stack, form, block, steps):
+    """The autotuner's other axes: the descent stack in shared memory, and each
+    job's rays grouped by octant before the launch (inside the graph)."""
+    jobs, dags, dev = small_batch
+    ref = [cbq.intersect_volume(g, o, d) for g, (o, d) in zip(dags, dev)]
+    batch = cbq.Batch([(g, o, d) for g, (o, d) in zip(dags, dev)])
+    batch.set_launch_config(block=block, refill_min=8, steps=steps, registers=registers, stack=stack, form=form)
+    cfg = batch.config()
+    assert (cfg["stack"], cfg["form"], cfg["registers"], cfg["steps"]) == (stack, form, registers, steps)
+    for rep in range(2):  # graph capture, then replay
+        for out in batch.outputs:
+            for v in out.values():
+                v.fill_(0x5A)
+        batch.launch()
+        torch.cuda.synchronize()
+        for j, (a, b) in enumerate(zip(batch.outputs, ref)):
+            for k in FIELDS:
+                assert _eq(a[k], b[k]), f"job {j} {k} (launch {rep})"
+    batch.destroy()
+
+
+def test_batch_rejects_bad_launch_config(small_batch):
+    jobs, dags, dev = small_batch
+    batch = cbq.Batch([(g, o, d) for g, (o, d) in zip(dags, dev)])
+    for kw in ({"block": 48}, {"refill_min": 0}, {"steps": 17}, {"registers": 48}, {"stack": 7}, {"form": 0}):
+        with pytest.raises(cbq.CbqError) as e:
+            batch.set_launch_config(**kw)
+        assert e.value.status == 1
+    batch.destroy()
+
+
 def test_batch_autotune_keeps_results(small_batch):
     jobs, dags, dev = small_batch
     ref = [cbq.intersect_volume(g, o, d) for g, (o, d) in zip(dags, dev)]
     batch = cbq.Batch([(g, o, d) for g, (o, d) in zip(dags, dev)])
     cfg = batch.autotune(1)
     assert cfg["block"] in (64, 128, 256) and cfg["refill_min"] in (4, 8, 12, 16)
+    assert cfg["steps"] in (4, 8, 16) and cfg["stack"] in (cbq.STACK_LOCAL, cbq.STACK_SHARED)
+    assert cfg["form"] in (cbq.FORM_PERSISTENT, cbq.FORM_SORTED)
     batch.launch()
     torch.cuda.synchronize()
     for a, b in zip(batch.outputs, ref):
