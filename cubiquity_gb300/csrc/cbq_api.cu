@@ -304,12 +304,14 @@ cbq_status cbq_dag_destroy(cbq_dag* dag)
 {
     if (!dag) return CBQ_ERR_INVALID_ARGUMENT;
     cudaFree(dag->d_nodes);
-    if (dag->d_stage) cudaFree(dag->d_stage);
     for (auto& kv : dag->stream_counters) cudaFree(kv.second);
-    for (cudaStream_t& st : dag->pipe)
-        if (st) cudaStreamDestroy(st);
-    for (cudaEvent_t& ev : dag->pipe_ev)
-        if (ev) cudaEventDestroy(ev);
+    for (auto& hs : dag->stages) {
+        if (hs->d_stage) cudaFree(hs->d_stage);
+        for (cudaStream_t& st : hs->pipe)
+            if (st) cudaStreamDestroy(st);
+        for (cudaEvent_t& ev : hs->pipe_ev)
+            if (ev) cudaEventDestroy(ev);
+    }
     delete dag;
     return CBQ_OK;
 }
@@ -556,42 +558,81 @@ cbq_status cbq_intersect_persistent(const cbq_dag* dag, const cbq_rays* rays, ui
     return cudaGetLastError() == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
 }
 
-cbq_status cbq_intersect_host(const cbq_dag* cdag, const float* host_origin_tmax, const float* host_direction,
-                              uint64_t n, const cbq_query* query, const cbq_hits* host_hits)
+}  // extern "C"
+
+namespace {
+
+// Takes a staging set of `dag` for one call, locked: a free one, else a new
+// one while fewer than kHostStagesMax exist, else the first (waiting for it).
+std::unique_lock<std::mutex> take_stage(cbq_dag* dag, HostStage** out)
+{
+    std::unique_lock<std::mutex> pool(dag->stages_lock);
+    for (auto& hs : dag->stages) {
+        std::unique_lock<std::mutex> lk(hs->lock, std::try_to_lock);
+        if (lk.owns_lock()) {
+            *out = hs.get();
+            return lk;
+        }
+    }
+    if ((int)dag->stages.size() < kHostStagesMax) {
+        HostStage* hs = new (std::nothrow) HostStage();
+        if (hs) {
+            dag->stages.emplace_back(hs);
+            *out = hs;
+            return std::unique_lock<std::mutex>(hs->lock);
+        }
+        if (dag->stages.empty()) {
+            *out = nullptr;
+            return std::unique_lock<std::mutex>();
+        }
+    }
+    HostStage* hs = dag->stages.front().get();
+    pool.unlock();
+    *out = hs;
+    return std::unique_lock<std::mutex>(hs->lock);
+}
+
+}  // namespace
+
+extern "C" cbq_status cbq_intersect_host(const cbq_dag* cdag, const float* host_origin_tmax,
+                                         const float* host_direction, uint64_t n, const cbq_query* query,
+                                         const cbq_hits* host_hits)
 {
     if (!cdag || !host_origin_tmax || !host_direction || !host_hits) return CBQ_ERR_INVALID_ARGUMENT;
     if (n == 0) return CBQ_OK;
     cbq_dag* dag = const_cast<cbq_dag*>(cdag);
-    std::lock_guard<std::mutex> lock(dag->staging_lock);
+    HostStage* hs = nullptr;
+    std::unique_lock<std::mutex> lock = take_stage(dag, &hs);
+    if (!hs) return CBQ_ERR_OUT_OF_MEMORY;
     // Staging: rays (32 B), hit fields (46 B) per ray, then one work counter per chunk.
     const size_t per_ray = 32 + 1 + 4 + 4 + 12 + 12 + 12 + 1;
     const size_t tail = 256 + kHostChunksMax * 64;
-    if (n > dag->stage_capacity) {
-        if (dag->d_stage) cudaFree(dag->d_stage);
-        dag->d_stage = nullptr;
-        dag->stage_capacity = 0;
-        if (cudaMalloc(&dag->d_stage, (size_t)n * per_ray + tail) != cudaSuccess) {
+    if (n > hs->capacity) {
+        if (hs->d_stage) cudaFree(hs->d_stage);
+        hs->d_stage = nullptr;
+        hs->capacity = 0;
+        if (cudaMalloc(&hs->d_stage, (size_t)n * per_ray + tail) != cudaSuccess) {
             cudaGetLastError();
             return CBQ_ERR_OUT_OF_MEMORY;
         }
-        dag->stage_capacity = n;
+        hs->capacity = n;
     }
-    if (!dag->pipe[0]) {  // created all together, or not at all
+    if (!hs->pipe[0]) {  // created all together, or not at all
         bool ok = true;
         for (int k = 0; k < 4 && ok; k++)
-            ok = cudaStreamCreateWithFlags(&dag->pipe[k], cudaStreamNonBlocking) == cudaSuccess;
+            ok = cudaStreamCreateWithFlags(&hs->pipe[k], cudaStreamNonBlocking) == cudaSuccess;
         for (uint64_t k = 0; k < 2 * kHostChunksMax && ok; k++)
-            ok = cudaEventCreateWithFlags(&dag->pipe_ev[k], cudaEventDisableTiming) == cudaSuccess;
+            ok = cudaEventCreateWithFlags(&hs->pipe_ev[k], cudaEventDisableTiming) == cudaSuccess;
         if (!ok) {
             cudaGetLastError();
-            for (cudaStream_t& st : dag->pipe)
+            for (cudaStream_t& st : hs->pipe)
                 if (st) { cudaStreamDestroy(st); st = nullptr; }
-            for (cudaEvent_t& ev : dag->pipe_ev)
+            for (cudaEvent_t& ev : hs->pipe_ev)
                 if (ev) { cudaEventDestroy(ev); ev = nullptr; }
             return CBQ_ERR_CUDA;
         }
     }
-    char* p = (char*)dag->d_stage;
+    char* p = (char*)hs->d_stage;
     float* d_o = (float*)p;
     p += n * 16;
     float* d_d = (float*)p;
@@ -613,11 +654,11 @@ cbq_status cbq_intersect_host(const cbq_dag* cdag, const float* host_origin_tmax
     // persistent launch ends with a tail of few busy warps).  Events order each chunk's copy in,
     // traversal and copy out.  Chunks interleave blocks of the batch (HostChunk).
     const uint64_t chunks = std::min<uint64_t>(kHostChunksMax, std::max<uint64_t>(1, n / kHostChunkMin));
-    cudaStream_t s_in = dag->pipe[0], s_out = dag->pipe[1];
+    cudaStream_t s_in = hs->pipe[0], s_out = hs->pipe[1];
     // Every queued copy and launch ends before the call returns (the staging buffers are reused).
     auto drain = [&](cbq_status st) {
         bool ok = true;
-        for (cudaStream_t s : dag->pipe) ok = cudaStreamSynchronize(s) == cudaSuccess && ok;
+        for (cudaStream_t s : hs->pipe) ok = cudaStreamSynchronize(s) == cudaSuccess && ok;
         return ok ? st : CBQ_ERR_CUDA;
     };
     const uint64_t block = std::max<uint64_t>(kHostBlockMin, n / (chunks * kHostBlocksPerChunk));
@@ -627,8 +668,8 @@ cbq_status cbq_intersect_host(const cbq_dag* cdag, const float* host_origin_tmax
         const uint64_t a = start, m = hc.rays();
         start += m;
         if (m == 0) continue;
-        cudaStream_t s_run = dag->pipe[2 + (k & 1)];
-        cudaEvent_t copied = dag->pipe_ev[2 * k], traversed = dag->pipe_ev[2 * k + 1];
+        cudaStream_t s_run = hs->pipe[2 + (k & 1)];
+        cudaEvent_t copied = hs->pipe_ev[2 * k], traversed = hs->pipe_ev[2 * k + 1];
         if (!copy_chunk((void*)host_origin_tmax, d_o, 16, hc, k, chunks, cudaMemcpyHostToDevice, s_in) ||
             !copy_chunk((void*)host_direction, d_d, 16, hc, k, chunks, cudaMemcpyHostToDevice, s_in) ||
             cudaEventRecord(copied, s_in) != cudaSuccess || cudaStreamWaitEvent(s_run, copied, 0) != cudaSuccess)
@@ -642,7 +683,7 @@ cbq_status cbq_intersect_host(const cbq_dag* cdag, const float* host_origin_tmax
         launch.voxel = host_hits->voxel ? dh.voxel + 3 * a : nullptr;
         launch.status = host_hits->status ? dh.status + a : nullptr;
         cbq_rays rays{d_o + 4 * a, d_d + 4 * a};
-        // Persistent form; each chunk's counter is private to this call (staging lock held).
+        // Persistent form; each chunk's counter is private to this call (its staging set is held).
         cbq_status st = cbq_intersect_persistent(dag, &rays, m, query, &launch, d_counters + 8 * k, 0u,
                                                  (cbq_stream_t)s_run);
         if (st != CBQ_OK) return drain(st);
@@ -665,5 +706,3 @@ cbq_status cbq_intersect_host(const cbq_dag* cdag, const float* host_origin_tmax
     }
     return drain(CBQ_OK);
 }
-
-}  // extern "C"

@@ -6,6 +6,7 @@
 
 #include <cstdint>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <vector>
 
@@ -47,6 +48,11 @@ cbq_status build_compact(const uint32_t* nodes, uint64_t node_count, const cbq_s
 // cbq_intersect_host_noalloc call.
 cbq_status noalloc_prepare(int device);
 
+// Calls of cbq_intersect_host on one DAG that overlap in time (from several
+// host threads) each take their own staging set, up to kHostStagesMax of them;
+// beyond that they queue for one.
+constexpr int kHostStagesMax = 4;
+
 // cbq_intersect_host splits a call into at most kHostChunksMax chunks of at
 // least kHostChunkMin rays.
 constexpr uint64_t kHostChunksMax = 8;
@@ -55,6 +61,17 @@ constexpr uint64_t kHostChunkMin = 1ull << 18;
 // kHostBlockMin) dealt round-robin.
 constexpr uint64_t kHostBlocksPerChunk = 4;
 constexpr uint64_t kHostBlockMin = 4096;
+
+// Device staging and streams of one cbq_intersect_host call at a time: rays and
+// hits, copied in and out in chunks on four streams (copy in, copy out, two for
+// traversal) so that copies overlap the traversal.
+struct HostStage {
+    std::mutex lock;               // held by the call using this set
+    void* d_stage = nullptr;
+    uint64_t capacity = 0;         // rays
+    struct CUstream_st* pipe[4] = {};  // cudaStream_t (this header is also compiled without CUDA)
+    struct CUevent_st* pipe_ev[2 * kHostChunksMax] = {};  // cudaEvent_t
+};
 
 }  // namespace cbq
 
@@ -75,15 +92,11 @@ struct cbq_dag {
     // 56-register kernel (also 2% faster for the city pathtracer's waves).
     cbq_launch_config cfg{CBQ_KERNEL_AUTO, 0, 0, 0, CBQ_STACK_LOCAL, CBQ_FORM_PERSISTENT, 8, 56};
 
-    // Staging for cbq_intersect_host: rays and hits, copied in and out in chunks on four
-    // streams (copy in, copy out, two for traversal) so that copies overlap the traversal.
-    std::mutex staging_lock;
-    void* d_stage = nullptr;
-    uint64_t stage_capacity = 0;   // rays
+    // Staging sets of cbq_intersect_host, created as concurrent calls need them.
+    std::mutex stages_lock;
+    std::vector<std::unique_ptr<cbq::HostStage>> stages;
     // Work counters of cbq_intersect's persistent form, one per stream id (ids are unique
     // for the context's lifetime, so launches sharing a counter are ordered by their stream).
     std::mutex counter_lock;
     std::map<unsigned long long, uint64_t*> stream_counters;
-    struct CUstream_st* pipe[4] = {};  // cudaStream_t (this header is also compiled without CUDA)
-    struct CUevent_st* pipe_ev[2 * cbq::kHostChunksMax] = {};  // cudaEvent_t
 };

@@ -234,9 +234,11 @@ cbq_status cbq_intersect(const cbq_dag* dag, const cbq_rays* rays, uint64_t n,
  * to 8 chunks whose copies overlap the traversal of their neighbours (own
  * streams; page-locked host buffers copy fastest); each chunk takes every k-th
  * of about 4k blocks of consecutive rays, so chunks carry even work.  Allocates
- * and caches device staging buffers per dag; calls on one dag are serialised by
- * a per-dag lock.  On an error every copy and launch it queued has ended before
- * it returns. */
+ * and caches device staging buffers and streams per dag.  Calls on one dag from
+ * several host threads run concurrently, each with its own staging set (up to
+ * four sets per dag, created as needed; further calls wait for one), so one
+ * call's copies and traversal overlap another's.  On an error every copy and
+ * launch it queued has ended before it returns. */
 cbq_status cbq_intersect_host(const cbq_dag* dag, const float* host_origin_tmax,
                               const float* host_direction, uint64_t n, const cbq_query* query,
                               const cbq_hits* host_hits);

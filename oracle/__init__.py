@@ -23,7 +23,6 @@ import numpy as np
 ORACLE_DIR = Path(__file__).resolve().parent
 ORACLE_LIB = ORACLE_DIR / "_build" / "liboracle.so"
 REF_LIB = ORACLE_DIR / "_ref" / "libcbq_ref.so"
-DEFAULT_REF_ROOT = Path(os.environ.get("CBQ_REFERENCE_ROOT", "/root/reference"))
 
 _P = ctypes.c_void_p
 _U64 = ctypes.c_uint64
@@ -41,12 +40,16 @@ class OrcHits(ctypes.Structure):
 
 
 def build(reference: bool | None = None) -> None:
-    """Builds liboracle.so, and _ref/libcbq_ref.so when the reference checkout exists."""
-    subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "all"], check=True)
+    """Builds liboracle.so, and _ref/libcbq_ref.so when the reference checkout
+    exists.  Where the checkout is, is the Makefile's business (its REF, which
+    CBQ_REFERENCE_ROOT in the environment overrides)."""
+    make = ["make", "-s", "-C", str(ORACLE_DIR)]
+    subprocess.run(make + ["all"], check=True)
     if reference is None:
-        reference = (DEFAULT_REF_ROOT / "src" / "library" / "raytracing.cpp").exists()
+        reference = subprocess.run(make + ["ref-check"], stdout=subprocess.DEVNULL,
+                                   stderr=subprocess.DEVNULL).returncode == 0
     if reference:
-        subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "ref", f"REF={DEFAULT_REF_ROOT}"], check=True)
+        subprocess.run(make + ["ref"], check=True)
 
 
 def reference_available() -> bool:
