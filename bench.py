@@ -904,7 +904,8 @@ def measure_serve(args, world, local, half_runs: int = 3, half_seconds: float = 
                 "generator_backpressure": r["backpressure"],
                 "generator_lateness_ms": {"p50": float(np.quantile(late, 0.5)) / 1e3,
                                           "p99": float(np.quantile(late, 0.99)) / 1e3,
-                                          "max": float(late.max()) / 1e3}}
+                                          "max": float(late.max()) / 1e3},
+                "submit_call_ms": {"p99": r["submit_p99_us"] / 1e3, "max": r["submit_max_us"] / 1e3}}
 
     clocks = ClockSampler(local)
     clocks.start()
@@ -925,7 +926,8 @@ def measure_serve(args, world, local, half_runs: int = 3, half_seconds: float = 
         "half_load": {"rate_rps": half["rate_rps"], "p50_ms": half["p50_ms"], "p99_ms": half["p99_ms"],
                       "p99_ms_runs": half["p99_ms_runs"], "seconds_per_run": half_seconds,
                       "mrays_per_s": half["mrays_per_s"], "requests_per_launch": half["requests_per_launch"],
-                      "generator_lateness_ms": half["generator_lateness_ms"]},
+                      "generator_lateness_ms": half["generator_lateness_ms"],
+                      "submit_call_ms": half["submit_call_ms"]},
         "latency": "submit -> hits in host memory, timed by the server; p99 = median over the runs",
         "arrivals": "open-loop Poisson, replayed by the library's native driver (cbq_server_replay)",
         "buffers": buffers, "clocks": clk,

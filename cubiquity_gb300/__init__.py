@@ -595,7 +595,8 @@ _sig("cbq_server_destroy", [_P])
 class _ReplayResult(ctypes.Structure):
     _fields_ = [("wall_seconds", ctypes.c_double), ("submitted", ctypes.c_uint64), ("failed", ctypes.c_uint64),
                 ("backpressure", ctypes.c_uint64), ("lateness_p50_us", ctypes.c_double),
-                ("lateness_p99_us", ctypes.c_double), ("lateness_max_us", ctypes.c_double)]
+                ("lateness_p99_us", ctypes.c_double), ("lateness_max_us", ctypes.c_double),
+                ("submit_p99_us", ctypes.c_double), ("submit_max_us", ctypes.c_double)]
 
 
 _sig("cbq_server_replay", [_P, _P, _P, _U64, _U32, _P, ctypes.POINTER(_ReplayResult)])

@@ -663,7 +663,7 @@ cbq_status cbq_server_replay(cbq_server* s, const cbq_request* requests, const d
     for (uint64_t k = 1; k < count; k++)
         if (!(arrival_s[k] >= arrival_s[k - 1])) return CBQ_ERR_INVALID_ARGUMENT;
     std::vector<uint64_t> tickets(count, 0);
-    std::vector<double> late(count, 0.0);
+    std::vector<double> late(count, 0.0), in_submit(count, 0.0);
     std::atomic<uint64_t> issued{0}, retired{0}, failed{0};
     std::atomic<bool> abort{false};
     // Waits for the requests in submission order; `retired` frees their buffers for reuse.
@@ -692,8 +692,10 @@ cbq_status cbq_server_replay(cbq_server* s, const cbq_request* requests, const d
             if (at - now > std::chrono::microseconds(300))
                 std::this_thread::sleep_for(at - now - std::chrono::microseconds(200));
         }
-        late[k] = std::chrono::duration<double, std::micro>(Clock::now() - at).count();
+        const Clock::time_point before = Clock::now();
+        late[k] = std::chrono::duration<double, std::micro>(before - at).count();
         st = cbq_server_submit(s, &requests[k], &tickets[k]);
+        in_submit[k] = std::chrono::duration<double, std::micro>(Clock::now() - before).count();
         if (st != CBQ_OK) break;
         issued.store(k + 1, std::memory_order_release);
     }
@@ -711,6 +713,8 @@ cbq_status cbq_server_replay(cbq_server* s, const cbq_request* requests, const d
         result->lateness_p50_us = percentile(late, 0.50);
         result->lateness_p99_us = percentile(late, 0.99);
         result->lateness_max_us = late.empty() ? 0.0 : *std::max_element(late.begin(), late.end());
+        result->submit_p99_us = percentile(in_submit, 0.99);
+        result->submit_max_us = in_submit.empty() ? 0.0 : *std::max_element(in_submit.begin(), in_submit.end());
     }
     return st;
 }

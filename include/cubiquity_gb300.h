@@ -418,6 +418,7 @@ typedef struct cbq_replay_result {
     double wall_seconds;            /* call start -> last completion */
     uint64_t submitted, failed, backpressure;
     double lateness_p50_us, lateness_p99_us, lateness_max_us;
+    double submit_p99_us, submit_max_us;   /* time spent inside cbq_server_submit */
 } cbq_replay_result;
 cbq_status cbq_server_replay(cbq_server* s, const cbq_request* requests, const double* arrival_s, uint64_t count,
                              uint32_t max_outstanding, double* lateness_us, cbq_replay_result* result);
