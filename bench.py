@@ -72,6 +72,9 @@ def parse_args():
     p.add_argument("--chunk", type=int, default=0, help="persistent: refill threshold (flat) / grab size (nested)")
     p.add_argument("--e2e-steps", type=int, default=20)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-impl", choices=["auto", "port"], default="auto",
+                   help="CPU ray cast timed by --impl reference: the reference's own library where it was built "
+                        "from the checkout (else the oracle's C restatement), or the restatement always")
     p.add_argument("--no-extras", action="store_true",
                    help="terrain-4096: skip the batch-64 and serve-8 measurements added to the line")
     p.add_argument("--layout", choices=["reference", "compact"], default="reference",
@@ -236,11 +239,13 @@ def max_over_ranks(world, value: float) -> float:
 
 # ------------------------------------------------------------------ CPU arms
 
-def cpu_trace(nodes, root, batches, threads=0):
-    """Times the reference CPU ray cast over the batches; returns (seconds, kind)."""
+def cpu_trace(nodes, root, batches, threads=0, impl="auto"):
+    """Times the reference CPU ray cast over the batches; returns (seconds, kind).
+    impl "auto": the reference's own library where it was built (oracle/_ref),
+    else the oracle's C restatement; "port": the restatement always."""
     import oracle
 
-    if oracle.reference_available():
+    if impl != "port" and oracle.reference_available():
         ref = oracle.Reference()
         vol = ref.volume_from_nodes(nodes, root)
         sd = vol.find_subdags()
@@ -291,11 +296,11 @@ def run_reference(args, world, rank):
         batches.append(("bounce", bo, bd))
     rays = sum(b[1].shape[0] for b in batches)
     for _ in range(args.warmup):
-        cpu_trace(nodes, root, batches)
+        cpu_trace(nodes, root, batches, impl=args.cpu_impl)
     total = 0.0
     kind = "port"
     for _ in range(args.steps):
-        dt, kind = cpu_trace(nodes, root, batches)
+        dt, kind = cpu_trace(nodes, root, batches, impl=args.cpu_impl)
         total += dt
     value = rays * args.steps / total / 1e6
     cores = host_cores()
