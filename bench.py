@@ -18,12 +18,12 @@ of the dominant launch against the L2 (the DAG is L2-resident; the same run
 measures the L2's read bandwidth and random-sector rate).  `fp64_error` compares
 the GPU's distances with the oracle's FP64 exact-box ray cast (CPU leg).
 
-On one GPU the default line also carries the benchmark's two other figures,
-measured after the terrain: `serve` (serve-8: peak request rate and p50/p99
-latency at half of it, median of three runs, with the load generator's
-lateness; measured by a child process, a server's own) and `batch` (batch-64:
-the batched persistent launch against the plain drop-in launched once per
-volume).  `--no-extras` skips them.
+On one GPU the default line also carries the benchmark's two other figures:
+`serve` (serve-8: peak request rate and p50/p99 latency at half of it, median
+of three runs, with the load generator's lateness; measured first, by a child
+process, alone on the GPU) and `batch` (batch-64: the batched persistent
+launch against the plain drop-in launched once per volume; measured after the
+terrain).  `--no-extras` skips them.
 
 Multi-GPU (torchrun, N > 1): replicas only.  Rays are independent and the DAG is
 read-only, so every rank traces its own full replica; there is no data-path
@@ -327,6 +327,12 @@ def run_gpu(args, world, rank, local):
     import torch
     import cubiquity_gb300 as cbq
 
+    # BASELINE's other two measurements ride on the default line (single-GPU
+    # runs): the serving latency (serve-8) first, by a child process, before
+    # this process creates its CUDA context; the batched form (batch-64) after
+    # the terrain.
+    extras = world == 1 and args.workload == "terrain-4096" and not args.no_extras
+    serve = serve_in_own_process(args, local) if extras else None
     torch.cuda.set_device(local)
     nodes, root, batches, bounce = make_workload(args.workload)
     dag = cbq.Dag(nodes, root, LAYOUTS[args.layout])
@@ -544,23 +550,20 @@ def run_gpu(args, world, rank, local):
         "fp64_error": fp64,
     }
     dag.destroy()
-    # BASELINE's other two measurements, on the same GPU after this one: the
-    # batched form against the plain drop-in (batch-64) and the serving latency
-    # (serve-8).  Single-GPU runs only.
-    if world == 1 and args.workload == "terrain-4096" and not args.no_extras:
-        line["serve"] = serve_in_own_process(args, local)
+    if extras:
+        line["serve"] = serve
         line["batch"] = measure_batch(args, world, local, e2e_steps=3)[0]
     if rank == 0:
         print(json.dumps(line), flush=True)
 
 
 def serve_in_own_process(args, local) -> dict:
-    """The serve-8 summary, measured by a child process.  A process that has
-    just freed large device allocations (this one, after the terrain leg) sees
-    completion latencies of several ms for tens of seconds afterwards (measured:
-    half-load p99 4.8-5.7 ms after creating and destroying a 4 GB server, 0.43 ms
-    without; a fresh process is unaffected), so the latency measurement runs
-    where a server runs: in a process of its own."""
+    """The serve-8 summary, measured by a child process before this one
+    touches the GPU.  After large device frees (by any process: this one's
+    terrain and batch legs free GBs) GPU completions are delayed by
+    milliseconds for tens of seconds (measured: half-load p99 4.4-7.2 ms
+    against 0.42-0.43 ms), so the latency is measured as a server runs: alone
+    on a GPU where nothing is being freed, in a process of its own."""
     cmd = [sys.executable, str(ROOT / "bench.py"), "--workload", "serve-8", "--serve-summary",
            "--serve-inflight", str(args.serve_inflight), "--serve-batch-rays", str(args.serve_batch_rays),
            "--serve-buffers", args.serve_buffers]
