@@ -255,8 +255,8 @@ cbq_status cbq_dag_create_ex(const uint32_t* host_nodes, uint64_t node_count, ui
     st = find_subdags(host_nodes, node_count, root, dag->subdags);
     if (st == CBQ_OK) st = validate_heights(host_nodes, node_count, dag->subdags);
     if (st != CBQ_OK) { delete dag; return st; }
-    dag->flat_ok = float_positions_exact(dag);
     dag->node_count = node_count;
+    dag->flat_ok = float_positions_exact(dag);
     dag->root = root;
     dag->max_height = 0;
     for (int i = 0; i < 8; i++)

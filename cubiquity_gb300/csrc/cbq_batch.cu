@@ -103,9 +103,9 @@ __device__ __forceinline__ void batch_body(const JobDesc* __restrict__ jobs, uin
         }
         lane_settle(L, c);
         if (SHARED)
-            lane_walk_steps(L, c, sstack, steps);
+            warp_walk_steps(L, c, sstack, steps);
         else
-            lane_walk_steps(L, c, lstack, steps);
+            warp_walk_steps(L, c, lstack, steps);
     }
 }
 

@@ -63,9 +63,9 @@ __device__ __forceinline__ void flat_body(const Ctx& c, uint64_t n, unsigned lon
         // Up to `steps` ESVO steps per outer iteration: amortises the refill
         // ballot and the settle check over several node fetches.
         if (SHARED)
-            lane_walk_steps(L, c, sstack, steps);
+            warp_walk_steps(L, c, sstack, steps);
         else
-            lane_walk_steps(L, c, lstack, steps);
+            warp_walk_steps(L, c, lstack, steps);
     }
 }
 
@@ -143,9 +143,11 @@ __global__ void __launch_bounds__(256) cbq_k_octant_scatter(const float4* __rest
 }  // namespace dev
 
 // True when every occupied SubDAG's reflected coordinates stay within
-// +-2^24, so the flat kernel's float positions are exact.
+// +-2^24, so the flat kernel's float positions are exact, and the store has
+// fewer than 2^29 nodes, so its word offsets fit 32 bits.
 bool float_positions_exact(const cbq_dag* dag)
 {
+    if (dag->node_count > dev::kFlatMaxNodes) return false;  // 32-bit node word offsets
     const int64_t lim = (int64_t)1 << 24;
     for (int i = 0; i < 8; i++) {
         const cbq_subdag& s = dag->subdags[i];

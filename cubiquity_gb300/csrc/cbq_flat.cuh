@@ -39,6 +39,7 @@ struct Lane {
     int h, start_h;
     float last_exit;
     uint32_t fetches, status, mode;
+    bool fast;                   // no slab distance can be NaN or -0: min/max need no NaN ordering
     uint32_t loads;              // node loads made (fetches minus skipped empty children)
     uint32_t job;                // batch kernel: index of the lane's job
     uint64_t ray;                // ray index within its job
@@ -105,6 +106,14 @@ __device__ __forceinline__ void lane_begin(Lane& L, const Src& c, uint64_t i)
     L.ix = __frcp_rn(rdx);
     L.iy = __frcp_rn(rdy);
     L.iz = __frcp_rn(rdz);
+    // With every |dir| component normal (>= FLT_MIN, not NaN) and a finite
+    // reflected origin, a slab distance (plane - o') * (1/|dir|) is a finite
+    // difference times a finite positive number: never NaN, and never -0
+    // (planes are floats of integers, so plane - o' is +0 when they are
+    // equal).  For such rays fminf/fmaxf give the bits of the reference's
+    // std::min/std::max compositions.
+    L.fast = rdx >= FLT_MIN && rdy >= FLT_MIN && rdz >= FLT_MIN && fabsf(L.rox) <= FLT_MAX &&
+             fabsf(L.roy) <= FLT_MAX && fabsf(L.roz) <= FLT_MAX;
     L.oct = 0u;
     L.ddx = (-L.rox) / rdx;
     L.ddy = (-L.roy) / rdy;
@@ -209,21 +218,36 @@ __device__ __forceinline__ void lane_enter(Lane& L, const Src& c)
     L.mode = kLaneWalk;
 }
 
+// min3/max3 of slab distances: the reference's NaN-ordered forms, or (FAST,
+// the lane's ray has Lane::fast) one fminf/fmaxf per pair, the same bits.
+template <bool FAST>
+__device__ __forceinline__ float slab_min3(float x, float y, float z)
+{
+    if constexpr (FAST) return fminf(fminf(x, y), z);
+    else return min3_ref(x, y, z);
+}
+template <bool FAST>
+__device__ __forceinline__ float slab_max3(float x, float y, float z)
+{
+    if constexpr (FAST) return fmaxf(fmaxf(x, y), z);
+    else return max3_ref(x, y, z);
+}
+
 // One iteration of the ESVO loop (raytracing.cpp:253-367).
-template <typename Src, typename Stack>
+template <bool FAST, typename Src, typename Stack>
 __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
 {
     const float c1x = ((L.fx + L.fcns) - L.rox) * L.ix;
     const float c1y = ((L.fy + L.fcns) - L.roy) * L.iy;
     const float c1z = ((L.fz + L.fcns) - L.roz) * L.iz;
-    const float tcx = min3_ref(c1x, c1y, c1z);
+    const float tcx = slab_min3<FAST>(c1x, c1y, c1z);
     const uint32_t child = child_of<Src::kCompact>(c.nodes(L), L.node, L.cid ^ L.sign, L.loads);
     L.fetches++;
     if (child > 0u) {
         const float c0x = (L.fx - L.rox) * L.ix;
         const float c0y = (L.fy - L.roy) * L.iy;
         const float c0z = (L.fz - L.roz) * L.iz;
-        const float tce = max3_ref(c0x, c0y, c0z);
+        const float tce = slab_max3<FAST>(c0x, c0y, c0z);
         if (child >= kMaterialCount && large_footprint(L.cns, tcx, c.query(L).max_footprint)) {
             if (tcx < L.last_exit) {
                 stack.put(L.h, L.node);
@@ -296,18 +320,29 @@ __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
 // the fetch budget spent (raytracing.cpp:253 with the cap): the steps here are
 // bounded by the budget left, and a lane still walking with the budget spent
 // ends exactly as that next step would have ended it.
-template <typename Src, typename Stack>
+template <bool FAST, typename Src, typename Stack>
 __device__ __forceinline__ void lane_walk_steps(Lane& L, const Src& c, Stack& stack, uint32_t steps)
 {
     if (L.mode != kLaneWalk) return;
     const uint32_t budget = kMaxFetches - L.fetches;  // > 0: a walking lane is below the cap
     // Every step makes one fetch, so the fetch count doubles as the step counter.
     const uint32_t end = L.fetches + (steps < budget ? steps : budget);
-    while (L.fetches < end && L.mode == kLaneWalk) lane_walk(L, c, stack);
+    while (L.fetches < end && L.mode == kLaneWalk) lane_walk<FAST>(L, c, stack);
     if (L.mode == kLaneWalk && L.fetches >= kMaxFetches) {
         L.status = kRayIterLimit;
         lane_finish(L, c, false, 0.0f, 0u, 0.0f, 0.0f, 0.0f);
     }
+}
+
+// The walk of a whole warp (all 32 lanes must call it): the FAST min/max when
+// every walking lane's ray allows it, else the reference's forms.
+template <typename Src, typename Stack>
+__device__ __forceinline__ void warp_walk_steps(Lane& L, const Src& c, Stack& stack, uint32_t steps)
+{
+    if (__all_sync(0xffffffffu, L.mode != kLaneWalk || L.fast))
+        lane_walk_steps<true>(L, c, stack, steps);
+    else
+        lane_walk_steps<false>(L, c, stack, steps);
 }
 
 // Octant transitions until the lane walks a SubDAG or has finished.  Bounded:

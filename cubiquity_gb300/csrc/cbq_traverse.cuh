@@ -21,6 +21,8 @@ namespace dev {
 
 constexpr uint32_t kMaterialCount = 256u;
 constexpr uint32_t kMaxFetches = 1u << 17;
+// The flat kernels index the node store with 32-bit word offsets.
+constexpr uint64_t kFlatMaxNodes = 1ull << 29;
 constexpr uint32_t kRayOk = 0u, kRayIterLimit = 1u, kRayStuck = 2u;
 
 struct SubDag {
@@ -72,6 +74,13 @@ __device__ __forceinline__ uint32_t load_child(const uint32_t* __restrict__ node
     return __ldg(nodes + ((size_t)node * 8u + slot));
 }
 
+// The same with the word index in 32 bits, for stores of fewer than 2^29
+// nodes (the flat kernels' condition, kFlatMaxNodes): one multiply-add less.
+__device__ __forceinline__ uint32_t load_child32(const uint32_t* __restrict__ nodes, uint32_t node, uint32_t slot)
+{
+    return __ldg(nodes + (node * 8u + slot));
+}
+
 // Child `slot` of node reference `node` in the compact store (the occupancy
 // mask is the reference's low byte, the packed children start at unit
 // node >> 8 of 8 bytes): an empty child costs no load.  `loads` counts loads.
@@ -81,10 +90,12 @@ __device__ __forceinline__ uint32_t load_child_compact(const uint32_t* __restric
     const uint32_t m = node & 0xffu;
     if (!((m >> slot) & 1u)) return 0u;
     loads++;
-    return __ldg(nodes + ((size_t)(node >> 8) * 2u + __popc(m & ((1u << slot) - 1u))));
+    return __ldg(nodes + ((node >> 8) * 2u + __popc(m & ((1u << slot) - 1u))));  // offsets < 2^25 words
 }
 
-template <bool COMPACT>
+// WIDE: 64-bit word index (the nested kernel, any store size); otherwise the
+// store has fewer than 2^29 nodes.
+template <bool COMPACT, bool WIDE = false>
 __device__ __forceinline__ uint32_t child_of(const uint32_t* __restrict__ nodes, uint32_t node, uint32_t slot,
                                              uint32_t& loads)
 {
@@ -92,7 +103,7 @@ __device__ __forceinline__ uint32_t child_of(const uint32_t* __restrict__ nodes,
         return load_child_compact(nodes, node, slot, loads);
     } else {
         loads++;
-        return load_child(nodes, node, slot);
+        return WIDE ? load_child(nodes, node, slot) : load_child32(nodes, node, slot);
     }
 }
 
@@ -152,7 +163,7 @@ struct EsvoOut {
 // findNearestMaterial (raytracing.cpp:134-162).
 // `fetches` counts child probes (the reference's loads, which also bound the
 // walk); `loads` the loads actually made (fewer in the compact layout).
-template <bool COMPACT = false>
+template <bool COMPACT = false, bool WIDE = false>
 __device__ __forceinline__ uint32_t nearest_material(const uint32_t* __restrict__ nodes, uint32_t node,
                                                      uint32_t sign_bits, uint32_t& fetches, uint32_t& status,
                                                      uint32_t& loads)
@@ -160,7 +171,7 @@ __device__ __forceinline__ uint32_t nearest_material(const uint32_t* __restrict_
     const uint32_t order = (0x76534210u | 0x88888888u) ^ (sign_bits * 0x11111111u);
     while (node >= kMaterialCount) {
         for (uint32_t ids = order; ids != 0u; ids >>= 4) {
-            const uint32_t c = child_of<COMPACT>(nodes, node, ids & 7u, loads);
+            const uint32_t c = child_of<COMPACT, WIDE>(nodes, node, ids & 7u, loads);
             fetches++;
             if (c > 0u) { node = c; break; }
         }
@@ -232,7 +243,7 @@ __device__ __forceinline__ EsvoOut esvo(const uint32_t* __restrict__ nodes, cons
                 res.distance = tce;
                 if (q.compute_surface) {
                     uint32_t loads = 0;
-                    res.material = nearest_material(nodes, child, f.sign_bits, fetches, status, loads);
+                    res.material = nearest_material<false, true>(nodes, child, f.sign_bits, fetches, status, loads);
                     if (status != kRayOk) { res.hit = false; return res; }
                     const float sx = (f.sign_bits & 1u) ? 1.0f : -1.0f;  // -rayDirSign
                     const float sy = (f.sign_bits & 2u) ? 1.0f : -1.0f;
