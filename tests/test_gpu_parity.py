@@ -353,3 +353,53 @@ def test_iteration_cap_inside_the_walk(orc):
                 scratch = cbq.scratch_for(o.shape[0])
                 got = _host(cbq.intersect_auto(dag, _dev(o), _dev(d), scratch))
                 _assert_same(got, want, FIELDS + ("status",), what=f"layout {layout} kernel {kernel} steps {steps}")
+
+
+def slab_boundary_rays(n=8192, seed=9):
+    """Rays on both sides of the condition under which the step takes min/max
+    with fminf/fmaxf (every |dir| component at least FLT_MIN, the reflected
+    origin finite): normal rays, components exactly FLT_MIN, subnormal and zero
+    components, huge, infinite and NaN origins, NaN directions.  Runs of 32
+    rays share a kind (so whole warps take either form) and single odd rays
+    sit among normal ones (so warps switch to the reference's form)."""
+    rng = np.random.default_rng(seed)
+    tiny = np.float32(np.finfo(np.float32).tiny)
+    o = np.zeros((n, 4), np.float32)
+    d = np.zeros((n, 4), np.float32)
+    o[:, :3] = rng.uniform(-20, 84, (n, 3))
+    o[:, 3] = np.inf
+    v = rng.normal(size=(n, 3))
+    d[:, :3] = v / np.linalg.norm(v, axis=1, keepdims=True)
+    kinds = rng.integers(0, 8, n // 32)
+    for r, k in enumerate(kinds):
+        sl = slice(32 * r, 32 * r + 32)
+        ax = rng.integers(0, 3)
+        if k == 1:
+            d[sl, ax] = np.copysign(tiny, d[sl, ax])               # exactly FLT_MIN: still the fast form
+        elif k == 2:
+            d[sl, ax] = np.copysign(tiny / 4, d[sl, ax])           # subnormal: 1/|d| overflows
+        elif k == 3:
+            d[sl, ax] = 0.0
+        elif k == 4:
+            o[sl, ax] = np.float32(3e38) * rng.choice([-1, 1])
+        elif k == 5:
+            o[sl, ax] = np.inf * rng.choice([-1, 1])
+        elif k == 6:
+            o[sl, ax] = np.nan
+    odd = rng.choice(n, n // 64, replace=False)                    # single odd lanes in normal warps
+    d[odd, 0] = rng.choice(np.array([0.0, tiny / 2, np.nan], np.float32), odd.size)
+    return o, d
+
+
+@pytest.mark.parametrize("form", [cbq.FORM_PLAIN, cbq.FORM_PERSISTENT])
+def test_slab_min_max_forms_at_their_boundary(orc, form):
+    nodes, root = W.SceneSpec(cbq.SCENE_SPHERES, 6, 11, 16).build()
+    o, d = slab_boundary_rays()
+    want = orc.intersect(nodes, orc.find_subdags(nodes, root), o, d)
+    assert want["hit"].sum() > 0
+    dag = cbq.Dag(nodes, root)
+    dag.set_launch_config(cbq.KERNEL_FLAT, 64, 0, 8, cbq.STACK_LOCAL, form, 8, 0)
+    scratch = cbq.scratch_for(o.shape[0])
+    got = _host(cbq.intersect_auto(dag, _dev(o), _dev(d), scratch))
+    _assert_same(got, want, FIELDS + ("status",), what="slab boundary")
+    dag.destroy()
