@@ -393,7 +393,7 @@ cbq_status cbq_dag_set_launch_config(cbq_dag* dag, const cbq_launch_config* cfg)
     if (cfg->refill_min > 32) return CBQ_ERR_INVALID_ARGUMENT;
     if (cfg->stack != CBQ_STACK_SHARED && cfg->stack != CBQ_STACK_LOCAL) return CBQ_ERR_INVALID_ARGUMENT;
     if (cfg->form < CBQ_FORM_PLAIN || cfg->form > CBQ_FORM_SORTED) return CBQ_ERR_INVALID_ARGUMENT;
-    if (cfg->steps < 0 || cfg->steps > 16) return CBQ_ERR_INVALID_ARGUMENT;
+    if (cfg->steps < 0 || cfg->steps > 32) return CBQ_ERR_INVALID_ARGUMENT;
     if (cfg->registers != 0 && cfg->registers != 56) return CBQ_ERR_INVALID_ARGUMENT;
     if (cfg->kernel == CBQ_KERNEL_NESTED && dag->layout == CBQ_DAG_LAYOUT_COMPACT) return CBQ_ERR_INVALID_ARGUMENT;
     dag->cfg = *cfg;
@@ -446,15 +446,16 @@ cbq_status cbq_autotune(cbq_dag* dag, const cbq_rays* rays, uint64_t n, const cb
     static const int blocks[] = {64, 128, 256};
     static const uint32_t refills[] = {4, 8, 16};
     static const int stacks[] = {CBQ_STACK_SHARED, CBQ_STACK_LOCAL};
-    static const int step_counts[] = {2, 4, 8, 16};
+    static const int step_counts[] = {2, 4, 8, 16, 32};
+    constexpr int kSteps = 5;
     for (int form = CBQ_FORM_PLAIN; form <= CBQ_FORM_SORTED && st == CBQ_OK; form++) {
         for (int blk : blocks) {
             for (uint32_t rf : refills) {
                 if (form == CBQ_FORM_PLAIN && rf != refills[0]) continue;  // refill unused
                 // stack x steps, plus the 56-register kernel for the persistent local-stack form
-                for (int v = 0; v < 12; v++) {
-                    const int stk = v < 8 ? stacks[v & 1] : CBQ_STACK_LOCAL;
-                    const int regs = v < 8 ? 0 : 56;
+                for (int v = 0; v < 3 * kSteps; v++) {
+                    const int stk = v < 2 * kSteps ? stacks[v & 1] : CBQ_STACK_LOCAL;
+                    const int regs = v < 2 * kSteps ? 0 : 56;
                     if (regs && form == CBQ_FORM_PLAIN) continue;
                     cbq_launch_config c = saved;
                     c.kernel = dag->flat_ok ? CBQ_KERNEL_FLAT : CBQ_KERNEL_NESTED;
@@ -462,7 +463,7 @@ cbq_status cbq_autotune(cbq_dag* dag, const cbq_rays* rays, uint64_t n, const cb
                     c.refill_min = rf;
                     c.stack = stk;
                     c.form = form;
-                    c.steps = v < 8 ? step_counts[v >> 1] : step_counts[v - 8];
+                    c.steps = v < 2 * kSteps ? step_counts[v >> 1] : step_counts[v - 2 * kSteps];
                     c.registers = regs;
                     dag->cfg = c;
                     st = cbq_intersect_auto(dag, rays, n, query, hits, scratch, scratch_bytes, stream);  // warm-up

@@ -399,7 +399,7 @@ cbq_status capture_graph(cbq_batch* b)
 cbq_status check_config(const cbq_batch_config& c)
 {
     if (c.block < 32 || c.block > 256 || (c.block % 32) != 0) return CBQ_ERR_INVALID_ARGUMENT;
-    if (c.refill_min < 1 || c.refill_min > 32 || c.steps < 1 || c.steps > 16) return CBQ_ERR_INVALID_ARGUMENT;
+    if (c.refill_min < 1 || c.refill_min > 32 || c.steps < 1 || c.steps > 32) return CBQ_ERR_INVALID_ARGUMENT;
     if (c.registers != 0 && c.registers != 56) return CBQ_ERR_INVALID_ARGUMENT;
     if (c.stack != CBQ_STACK_LOCAL && c.stack != CBQ_STACK_SHARED) return CBQ_ERR_INVALID_ARGUMENT;
     if (c.form != CBQ_FORM_PERSISTENT && c.form != CBQ_FORM_SORTED) return CBQ_ERR_INVALID_ARGUMENT;

@@ -182,7 +182,7 @@ typedef struct cbq_launch_config {
     uint32_t refill_min;      /* flat persistent: idle lanes that trigger a refill, 0 = default */
     int32_t stack;            /* CBQ_STACK_* (flat kernel) */
     int32_t form;             /* CBQ_FORM_*, used by cbq_intersect_auto */
-    int32_t steps;            /* flat kernel: ESVO steps per loop iteration (1..16), 0 = 1 */
+    int32_t steps;            /* flat kernel: ESVO steps per loop iteration (1..32), 0 = 1 */
     int32_t registers;        /* 0, or 56 (the default): the persistent local-stack
                                  kernel held to 56 registers per thread (more
                                  resident warps); other forms ignore it */
@@ -202,7 +202,7 @@ cbq_status cbq_intersect_auto(const cbq_dag* dag, const cbq_rays* rays, uint64_t
                               const cbq_hits* hits, void* scratch, uint64_t scratch_bytes, cbq_stream_t stream);
 
 /* Autotuner: times every form x block {64,128,256} x refill {4,8,16} x stack
- * {shared, local} x steps {2,4,8,16}, and the 56-register persistent
+ * {shared, local} x steps {2,4,8,16,32}, and the 56-register persistent
  * local-stack kernel, on these rays (synchronous; `repetitions` launches each),
  * stores the fastest in the DAG's launch config and returns it with its time. */
 cbq_status cbq_autotune(cbq_dag* dag, const cbq_rays* rays, uint64_t n, const cbq_query* query,
@@ -308,7 +308,7 @@ cbq_status cbq_batch_get_config(const cbq_batch* b, int32_t* block, uint32_t* re
 typedef struct cbq_batch_config {
     int32_t block;            /* threads per block: 32..256, a multiple of 32 */
     uint32_t refill_min;      /* idle lanes that trigger a warp's refill: 1..32 */
-    int32_t steps;            /* ESVO steps per loop iteration: 1..16 */
+    int32_t steps;            /* ESVO steps per loop iteration: 1..32 */
     int32_t registers;        /* 0, or 56: the local-stack kernel held to 56 registers */
     int32_t stack;            /* CBQ_STACK_LOCAL or CBQ_STACK_SHARED (descent stack placement) */
     int32_t form;             /* CBQ_FORM_PERSISTENT: rays in the order given; CBQ_FORM_SORTED: each

@@ -114,7 +114,7 @@ def test_batch_stack_and_octant_order_do_not_change_results(small_batch, registe
 def test_batch_rejects_bad_launch_config(small_batch):
     jobs, dags, dev = small_batch
     batch = cbq.Batch([(g, o, d) for g, (o, d) in zip(dags, dev)])
-    for kw in ({"block": 48}, {"refill_min": 0}, {"steps": 17}, {"registers": 48}, {"stack": 7}, {"form": 0}):
+    for kw in ({"block": 48}, {"refill_min": 0}, {"steps": 33}, {"registers": 48}, {"stack": 7}, {"form": 0}):
         with pytest.raises(cbq.CbqError) as e:
             batch.set_launch_config(**kw)
         assert e.value.status == 1
