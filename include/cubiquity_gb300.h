@@ -380,7 +380,10 @@ typedef struct cbq_server_stats {
  * budget and a launch slot allow, grouped into one persistent multi-volume
  * launch per group, and launched while earlier groups still run; launches are
  * completed in the order they finish.  Each result equals cbq_intersect_host
- * on that request alone. */
+ * on that request alone.  A server runs two threads: a scheduler, asleep
+ * unless requests queue, and a completion thread that polls the events of the
+ * launches in flight (yielding between rounds), so it keeps one host core busy
+ * while the GPU has work from the server and sleeps otherwise. */
 typedef struct cbq_server cbq_server;
 
 cbq_status cbq_server_create(const cbq_server_config* cfg, cbq_server** out);
