@@ -487,9 +487,14 @@ def run_gpu(args, world, rank, local):
     # and its hits copied out.  The single-thread figure (the batches' calls one
     # after the other) is kept beside it.
     def e2e_timed(threaded: bool) -> float:
+        errors = []
+
         def worker(h):
-            for _ in range(args.e2e_steps):
-                e2e_call(h)
+            try:
+                for _ in range(args.e2e_steps):
+                    e2e_call(h)
+            except Exception as e:  # noqa: BLE001  (re-raised below: a failed call voids the figure)
+                errors.append(e)
         for h in host:  # warm-up: staging sets allocated
             e2e_call(h)
         barrier(world)
@@ -500,6 +505,8 @@ def run_gpu(args, world, rank, local):
                 x.start()
             for x in th:
                 x.join()
+            if errors:
+                raise errors[0]
         else:
             for _ in range(args.e2e_steps):
                 for h in host:
