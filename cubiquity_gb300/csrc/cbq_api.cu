@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <exception>
 #include <new>
 #include <vector>
 
@@ -578,7 +579,14 @@ std::unique_lock<std::mutex> take_stage(cbq_dag* dag, HostStage** out)
     if ((int)dag->stages.size() < kHostStagesMax) {
         HostStage* hs = new (std::nothrow) HostStage();
         if (hs) {
-            dag->stages.emplace_back(hs);
+            try {
+                dag->stages.emplace_back(hs);
+            } catch (const std::exception&) {  // nothing may throw across the C ABI
+                delete hs;
+                hs = nullptr;
+            }
+        }
+        if (hs) {
             *out = hs;
             return std::unique_lock<std::mutex>(hs->lock);
         }

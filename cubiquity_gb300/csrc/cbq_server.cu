@@ -23,6 +23,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <exception>
 #include <map>
 #include <mutex>
 #include <new>
@@ -493,8 +494,17 @@ cbq_status cbq_server_create(const cbq_server_config* cfg, cbq_server** out)
         cbq_server_destroy(s);
         return CBQ_ERR_OUT_OF_MEMORY;
     }
-    s->scheduler = std::thread([s] { s->run_scheduler(); });
-    s->completer = std::thread([s] { s->run_completer(); });
+    try {
+        s->scheduler = std::thread([s] { s->run_scheduler(); });
+        s->completer = std::thread([s] { s->run_completer(); });
+    } catch (const std::exception&) {  // no thread: nothing may throw across the C ABI
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->stopping = true;
+        }
+        cbq_server_destroy(s);
+        return CBQ_ERR_OUT_OF_MEMORY;
+    }
     *out = s;
     return CBQ_OK;
 }
@@ -662,12 +672,20 @@ cbq_status cbq_server_replay(cbq_server* s, const cbq_request* requests, const d
     if (!s || (count > 0 && (!requests || !arrival_s)) || max_outstanding == 0) return CBQ_ERR_INVALID_ARGUMENT;
     for (uint64_t k = 1; k < count; k++)
         if (!(arrival_s[k] >= arrival_s[k - 1])) return CBQ_ERR_INVALID_ARGUMENT;
-    std::vector<uint64_t> tickets(count, 0);
-    std::vector<double> late(count, 0.0), in_submit(count, 0.0);
+    std::vector<uint64_t> tickets;
+    std::vector<double> late, in_submit;
+    try {
+        tickets.assign(count, 0);
+        late.assign(count, 0.0);
+        in_submit.assign(count, 0.0);
+    } catch (const std::exception&) {
+        return CBQ_ERR_OUT_OF_MEMORY;
+    }
     std::atomic<uint64_t> issued{0}, retired{0}, failed{0};
     std::atomic<bool> abort{false};
     // Waits for the requests in submission order; `retired` frees their buffers for reuse.
-    std::thread waiter([&] {
+    std::thread waiter;
+    auto wait_in_order = [&] {
         for (uint64_t k = 0; k < count; k++) {
             while (issued.load(std::memory_order_acquire) <= k) {
                 if (abort.load(std::memory_order_acquire)) return;
@@ -676,7 +694,12 @@ cbq_status cbq_server_replay(cbq_server* s, const cbq_request* requests, const d
             if (cbq_server_wait(s, tickets[k], -1) != CBQ_OK) failed.fetch_add(1);
             retired.store(k + 1, std::memory_order_release);
         }
-    });
+    };
+    try {
+        waiter = std::thread(wait_in_order);
+    } catch (const std::exception&) {
+        return CBQ_ERR_OUT_OF_MEMORY;  // nothing submitted yet
+    }
     uint64_t backpressure = 0;
     cbq_status st = CBQ_OK;
     const Clock::time_point t0 = Clock::now();
