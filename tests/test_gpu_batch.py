@@ -168,3 +168,27 @@ def test_batch_rejects_bad_jobs(small_batch):
     assert cbq.lib().cbq_batch_create(arr, 1, None, ctypes.byref(h)) == 1
     arr[0].dag = None
     assert cbq.lib().cbq_batch_create(arr, 1, None, ctypes.byref(h)) == 1
+
+
+@pytest.mark.parametrize("stack,form", [(cbq.STACK_LOCAL, cbq.FORM_PERSISTENT), (cbq.STACK_SHARED, cbq.FORM_SORTED)])
+def test_batch_lod_and_tmax_query(small_batch, stack, form):
+    """The batch's query applies to every job: with a LOD footprint the walk
+    stops above the leaves (findNearestMaterial picks the material) and with
+    tmax the far hits become misses, exactly as on the single-volume path."""
+    jobs, dags, dev = small_batch
+    kw = dict(compute_surface_properties=True, max_footprint=0.02, use_tmax=True)
+    tmaxed = []
+    for o, d in dev:
+        o2 = o.clone()
+        o2[:, 3] = 40.0
+        tmaxed.append((o2, d))
+    ref = [cbq.intersect_volume(g, o, d, **kw) for g, (o, d) in zip(dags, tmaxed)]
+    batch = cbq.Batch([(g, o, d) for g, (o, d) in zip(dags, tmaxed)], **kw)
+    batch.set_launch_config(block=128, refill_min=8, steps=8, registers=0, stack=stack, form=form)
+    batch.launch()
+    torch.cuda.synchronize()
+    for j, (a, b) in enumerate(zip(batch.outputs, ref)):
+        for k in FIELDS:
+            assert _eq(a[k], b[k]), f"job {j} {k}"
+    assert any(int(r["hit"].sum()) > 0 for r in ref)
+    batch.destroy()
