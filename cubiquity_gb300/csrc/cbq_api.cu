@@ -20,7 +20,7 @@ constexpr uint32_t kRefillDefault = 8;
 
 bool use_flat(const cbq_dag* dag)
 {
-    return dag->flat_ok && (dag->cfg.kernel != CBQ_KERNEL_NESTED || dag->layout == CBQ_DAG_LAYOUT_COMPACT);
+    return dag->cfg.kernel != CBQ_KERNEL_NESTED || dag->layout == CBQ_DAG_LAYOUT_COMPACT;
 }
 
 int flat_block(const cbq_dag* dag) { return dag->cfg.block > 0 ? dag->cfg.block : kFlatBlockDefault; }
@@ -296,7 +296,7 @@ cbq_status cbq_dag_create_ex(const uint32_t* host_nodes, uint64_t node_count, ui
              "DAG uploaded to device %d: %llu nodes, %s layout (%.1f MB), root %u, max sub-DAG height %d, %s kernel",
              dag->device, (unsigned long long)node_count,
              dag->layout == CBQ_DAG_LAYOUT_COMPACT ? "compact" : "reference", bytes / 1e6, root, dag->max_height,
-             dag->flat_ok ? "flat" : "nested (coordinates beyond 2^24)");
+             dag->flat_ok ? "flat (float positions)" : "flat (integer positions: coordinates beyond 2^24 or 2^29 nodes)");
     *out = dag;
     return CBQ_OK;
 }
@@ -459,8 +459,8 @@ cbq_status cbq_autotune(cbq_dag* dag, const cbq_rays* rays, uint64_t n, const cb
                     const int regs = v < 2 * kSteps ? 0 : 56;
                     if (regs && form == CBQ_FORM_PLAIN) continue;
                     cbq_launch_config c = saved;
-                    c.kernel = dag->flat_ok ? CBQ_KERNEL_FLAT : CBQ_KERNEL_NESTED;
-                    c.block = dag->flat_ok ? blk : 0;
+                    c.kernel = CBQ_KERNEL_FLAT;
+                    c.block = blk;
                     c.refill_min = rf;
                     c.stack = stk;
                     c.form = form;
@@ -478,7 +478,6 @@ cbq_status cbq_autotune(cbq_dag* dag, const cbq_rays* rays, uint64_t n, const cb
                     cudaEventElapsedTime(&ms, e0, e1);
                     ms /= (float)repetitions;
                     if (ms < win_ms) { win_ms = ms; winner = c; }
-                    if (!dag->flat_ok) break;  // the nested kernel has no stack choice
                 }
                 if (st != CBQ_OK) break;
             }
@@ -502,7 +501,7 @@ cbq_status cbq_dag_get_launch_config(const cbq_dag* dag, cbq_launch_config* cfg)
 {
     if (!dag || !cfg) return CBQ_ERR_INVALID_ARGUMENT;
     *cfg = dag->cfg;
-    if (cfg->kernel == CBQ_KERNEL_AUTO) cfg->kernel = dag->flat_ok ? CBQ_KERNEL_FLAT : CBQ_KERNEL_NESTED;
+    if (cfg->kernel == CBQ_KERNEL_AUTO) cfg->kernel = CBQ_KERNEL_FLAT;
     if (cfg->block == 0) cfg->block = use_flat(dag) ? kFlatBlockDefault : kPlainBlock;
     if (cfg->chunk == 0) cfg->chunk = kDefaultChunk;
     if (cfg->refill_min == 0) cfg->refill_min = kRefillDefault;

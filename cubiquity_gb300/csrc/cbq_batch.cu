@@ -20,6 +20,7 @@ namespace dev {
 template <bool COMPACT>
 struct BatchSrc {
     static constexpr bool kCompact = COMPACT;
+    static constexpr bool kIntPos = false;  // jobs whose DAG needs integer positions run on their own
     const JobDesc* __restrict__ jobs;
 
     __device__ __forceinline__ const QueryParams& query(const Lane& L) const { return jobs[L.job].q; }
@@ -293,7 +294,7 @@ constexpr uint32_t kBatchRefillDefault = 8;
 struct cbq_batch {
     int device = 0;
     std::vector<cbq_job> jobs;              // as given (host copy)
-    std::vector<int> nested_jobs;           // jobs whose DAG needs the nested kernel
+    std::vector<int> nested_jobs;           // jobs whose DAG needs integer positions (launched on their own)
     dev::JobDesc* d_jobs = nullptr;         // reference-layout jobs, then compact-layout jobs
     uint32_t njobs = 0;                     // jobs in the device table
     uint32_t njobs_ref = 0;                 // of which reference layout (one launch per layout)

@@ -182,7 +182,8 @@ bool query_persistent_kernels()
 // memory).  Done for every persistent traversal kernel when a DAG is created.
 cbq_status preload_persistent_kernels()
 {
-    const bool ok = query_persistent_kernels<dev::FlatCtxT<false>>() && query_persistent_kernels<dev::FlatCtxT<true>>();
+    const bool ok = query_persistent_kernels<dev::FlatCtxT<false>>() && query_persistent_kernels<dev::FlatCtxT<true>>() &&
+                    query_persistent_kernels<dev::FlatCtxT<false, false, true>>();
     if (!ok) cudaGetLastError();
     return ok ? CBQ_OK : CBQ_ERR_CUDA;
 }
@@ -280,11 +281,18 @@ cbq_status launch_flat(const cbq_dag* dag, const dev::DagParams& dp, const dev::
         if (dag->layout == CBQ_DAG_LAYOUT_COMPACT)
             return launch_variant<false, false, false>(
                 make_ctx<dev::FlatCtxT<true, true>>(dp, q, out, orig, dir, fetch_out), n, one, rows, stream, dv);
+        if (!dag->flat_ok)
+            return launch_variant<false, false, false>(
+                make_ctx<dev::FlatCtxT<false, true, true>>(dp, q, out, orig, dir, fetch_out), n, one, rows, stream,
+                dv);
         return launch_variant<false, false, false>(
             make_ctx<dev::FlatCtxT<false, true>>(dp, q, out, orig, dir, fetch_out), n, one, rows, stream, dv);
     }
     if (dag->layout == CBQ_DAG_LAYOUT_COMPACT)
         return launch_ctx(make_ctx<dev::FlatCtxT<true>>(dp, q, out, orig, dir, nullptr), n, fl, rows, stream, dv);
+    if (!dag->flat_ok)  // coordinates beyond +-2^24 or 2^29 nodes or more: integer positions
+        return launch_ctx(make_ctx<dev::FlatCtxT<false, false, true>>(dp, q, out, orig, dir, nullptr), n, fl, rows,
+                          stream, dv);
     return launch_ctx(make_ctx<dev::FlatCtxT<false>>(dp, q, out, orig, dir, nullptr), n, fl, rows, stream, dv);
 }
 

@@ -35,7 +35,8 @@ struct Lane {
     // ESVO walk state
     uint32_t node, cid, written;
     int32_t cns;
-    float fx, fy, fz, fcns;
+    float fx, fy, fz, fcns;      // child position and size as exact floats (float-position form)
+    int32_t px, py, pz;          // child position as wrapping i32 (integer-position form)
     int h, start_h;
     float last_exit;
     uint32_t fetches, status, mode;
@@ -53,9 +54,14 @@ struct Lane {
 // which writes per ray the node loads (child probes in the reference layout,
 // fewer in the compact one) to fetch_out.  It is a separate instantiation, so
 // the traversal kernels carry no counting code (measured: 1-2% faster).
-template <bool COMPACT, bool COUNT_LOADS = false>
+template <bool COMPACT, bool COUNT_LOADS = false, bool INT_POS = false>
 struct FlatCtxT {
     static constexpr bool kCompact = COMPACT;
+    // INT_POS: child positions as wrapping i32 converted to float where a slab
+    // plane is needed (the reference's own arithmetic, any coordinates, 64-bit
+    // node offsets); otherwise exact floats (coordinates within +-2^24, fewer
+    // than 2^29 nodes).
+    static constexpr bool kIntPos = INT_POS;
     DagParams dag;
     QueryParams q;
     HitsOut out;
@@ -208,11 +214,18 @@ __device__ __forceinline__ void lane_enter(Lane& L, const Src& c)
     L.h = s.height;
     L.node = s.node;
     L.cns = (int32_t)(ns >> 1);
-    L.fcns = (float)L.cns;
-    L.cid = first_child_f(L, entry, fpx + L.fcns, fpy + L.fcns, fpz + L.fcns);
-    L.fx = fpx + ((L.cid & 1u) ? L.fcns : 0.0f);
-    L.fy = fpy + ((L.cid & 2u) ? L.fcns : 0.0f);
-    L.fz = fpz + ((L.cid & 4u) ? L.fcns : 0.0f);
+    if constexpr (Src::kIntPos) {
+        L.cid = first_child_f(L, entry, (float)wadd(px, L.cns), (float)wadd(py, L.cns), (float)wadd(pz, L.cns));
+        L.px = wadd(px, (L.cid & 1u) ? L.cns : 0);
+        L.py = wadd(py, (L.cid & 2u) ? L.cns : 0);
+        L.pz = wadd(pz, (L.cid & 4u) ? L.cns : 0);
+    } else {
+        L.fcns = (float)L.cns;
+        L.cid = first_child_f(L, entry, fpx + L.fcns, fpy + L.fcns, fpz + L.fcns);
+        L.fx = fpx + ((L.cid & 1u) ? L.fcns : 0.0f);
+        L.fy = fpy + ((L.cid & 2u) ? L.fcns : 0.0f);
+        L.fz = fpz + ((L.cid & 4u) ? L.fcns : 0.0f);
+    }
     L.last_exit = exit_;
     L.written = 0u;
     L.mode = kLaneWalk;
@@ -237,16 +250,18 @@ __device__ __forceinline__ float slab_max3(float x, float y, float z)
 template <bool FAST, typename Src, typename Stack>
 __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
 {
-    const float c1x = ((L.fx + L.fcns) - L.rox) * L.ix;
-    const float c1y = ((L.fy + L.fcns) - L.roy) * L.iy;
-    const float c1z = ((L.fz + L.fcns) - L.roz) * L.iz;
+    constexpr bool INT = Src::kIntPos;
+    // Exit planes: vec3(childPos + childNodeSize) (raytracing.cpp:259-260).
+    const float c1x = ((INT ? (float)wadd(L.px, L.cns) : L.fx + L.fcns) - L.rox) * L.ix;
+    const float c1y = ((INT ? (float)wadd(L.py, L.cns) : L.fy + L.fcns) - L.roy) * L.iy;
+    const float c1z = ((INT ? (float)wadd(L.pz, L.cns) : L.fz + L.fcns) - L.roz) * L.iz;
     const float tcx = slab_min3<FAST>(c1x, c1y, c1z);
-    const uint32_t child = child_of<Src::kCompact>(c.nodes(L), L.node, L.cid ^ L.sign, L.loads);
+    const uint32_t child = child_of<Src::kCompact, INT>(c.nodes(L), L.node, L.cid ^ L.sign, L.loads);
     L.fetches++;
     if (child > 0u) {
-        const float c0x = (L.fx - L.rox) * L.ix;
-        const float c0y = (L.fy - L.roy) * L.iy;
-        const float c0z = (L.fz - L.roz) * L.iz;
+        const float c0x = ((INT ? (float)L.px : L.fx) - L.rox) * L.ix;
+        const float c0y = ((INT ? (float)L.py : L.fy) - L.roy) * L.iy;
+        const float c0z = ((INT ? (float)L.pz : L.fz) - L.roz) * L.iz;
         const float tce = slab_max3<FAST>(c0x, c0y, c0z);
         if (child >= kMaterialCount && large_footprint(L.cns, tcx, c.query(L).max_footprint)) {
             if (tcx < L.last_exit) {
@@ -257,16 +272,25 @@ __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
             L.h--;
             L.node = child;
             L.cns >>= 1;
-            L.fcns = (float)L.cns;
-            L.cid = first_child_f(L, tce, L.fx + L.fcns, L.fy + L.fcns, L.fz + L.fcns);
-            if (L.cid & 1u) L.fx += L.fcns;
-            if (L.cid & 2u) L.fy += L.fcns;
-            if (L.cid & 4u) L.fz += L.fcns;
+            if constexpr (INT) {
+                L.cid = first_child_f(L, tce, (float)wadd(L.px, L.cns), (float)wadd(L.py, L.cns),
+                                      (float)wadd(L.pz, L.cns));
+                if (L.cid & 1u) L.px = wadd(L.px, L.cns);
+                if (L.cid & 2u) L.py = wadd(L.py, L.cns);
+                if (L.cid & 4u) L.pz = wadd(L.pz, L.cns);
+            } else {
+                L.fcns = (float)L.cns;
+                L.cid = first_child_f(L, tce, L.fx + L.fcns, L.fy + L.fcns, L.fz + L.fcns);
+                if (L.cid & 1u) L.fx += L.fcns;
+                if (L.cid & 2u) L.fy += L.fcns;
+                if (L.cid & 4u) L.fz += L.fcns;
+            }
         } else {
             uint32_t material = 0u;
             float nx = 0.0f, ny = 0.0f, nz = 0.0f;
             if (c.query(L).compute_surface) {
-                material = nearest_material<Src::kCompact>(c.nodes(L), child, L.sign, L.fetches, L.status, L.loads);
+                material = nearest_material<Src::kCompact, INT>(c.nodes(L), child, L.sign, L.fetches, L.status,
+                                                                L.loads);
                 if (L.status != kRayOk) {
                     lane_finish(L, c, false, 0.0f, 0u, 0.0f, 0.0f, 0.0f);
                     return;
@@ -286,16 +310,26 @@ __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
         return;
     }
     L.cid ^= flips;
-    if (flips & 1u) L.fx += L.fcns;
-    if (flips & 2u) L.fy += L.fcns;
-    if (flips & 4u) L.fz += L.fcns;
+    if constexpr (INT) {
+        if (flips & 1u) L.px = wadd(L.px, L.cns);
+        if (flips & 2u) L.py = wadd(L.py, L.cns);
+        if (flips & 4u) L.pz = wadd(L.pz, L.cns);
+    } else {
+        if (flips & 1u) L.fx += L.fcns;
+        if (flips & 2u) L.fy += L.fcns;
+        if (flips & 4u) L.fz += L.fcns;
+    }
     if ((L.cid & flips) != flips) {
-        // Integer positions from the exact float ones (|p| < 2^24); on a flipped axis the
-        // position before the advance was p - childSize.
-        const int32_t cx = __float2int_rz(L.fx), cy = __float2int_rz(L.fy), cz = __float2int_rz(L.fz);
-        const uint32_t diff = ((flips & 1u) ? (uint32_t)(cx ^ (cx - L.cns)) : 0u) |
-                              ((flips & 2u) ? (uint32_t)(cy ^ (cy - L.cns)) : 0u) |
-                              ((flips & 4u) ? (uint32_t)(cz ^ (cz - L.cns)) : 0u);
+        // Integer positions: the wrapping i32 ones, or from the exact float ones
+        // (|p| < 2^24).  On a flipped axis the position before the advance was
+        // p - childSize.
+        const int32_t cx = INT ? L.px : __float2int_rz(L.fx);
+        const int32_t cy = INT ? L.py : __float2int_rz(L.fy);
+        const int32_t cz = INT ? L.pz : __float2int_rz(L.fz);
+        const uint32_t cs = (uint32_t)L.cns;
+        const uint32_t diff = ((flips & 1u) ? ((uint32_t)cx ^ ((uint32_t)cx - cs)) : 0u) |
+                              ((flips & 2u) ? ((uint32_t)cy ^ ((uint32_t)cy - cs)) : 0u) |
+                              ((flips & 4u) ? ((uint32_t)cz ^ ((uint32_t)cz - cs)) : 0u);
         const int msb = 31 - __clz(diff);
         const int h = msb + 1;
         if (h > L.start_h) {  // left the sub-DAG: on to the next octant
@@ -305,13 +339,19 @@ __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
         L.h = h;
         L.node = (L.written & (1u << h)) ? stack.get(h) : 0u;
         L.cns = (int32_t)(1u << msb);
-        L.fcns = (float)L.cns;
         L.cid = (((uint32_t)cx >> msb) & 1u) | ((((uint32_t)cy >> msb) & 1u) << 1) |
                 ((((uint32_t)cz >> msb) & 1u) << 2);
         const uint32_t keep = 0u - (uint32_t)L.cns;
-        L.fx = (float)(int32_t)((uint32_t)cx & keep);
-        L.fy = (float)(int32_t)((uint32_t)cy & keep);
-        L.fz = (float)(int32_t)((uint32_t)cz & keep);
+        if constexpr (INT) {
+            L.px = (int32_t)((uint32_t)cx & keep);
+            L.py = (int32_t)((uint32_t)cy & keep);
+            L.pz = (int32_t)((uint32_t)cz & keep);
+        } else {
+            L.fcns = (float)L.cns;
+            L.fx = (float)(int32_t)((uint32_t)cx & keep);
+            L.fy = (float)(int32_t)((uint32_t)cy & keep);
+            L.fz = (float)(int32_t)((uint32_t)cz & keep);
+        }
         L.last_exit = 0.0f;
     }
 }

@@ -86,7 +86,8 @@ struct cbq_dag {
     cbq_subdag subdags[8];
     int32_t max_height = 0;        // max SubDAG height (stack depth)
     int device = 0;
-    bool flat_ok = false;          // float positions exact (coordinates within +-2^24)
+    bool flat_ok = false;          // float-position flat kernel applies (coordinates within +-2^24,
+                                   // under 2^29 nodes); otherwise the integer-position form
     // Defaults from the GB300 sweep on terrain-4096 (primary and bounce rays):
     // persistent refill, stack in local memory, 8 ESVO steps per loop iteration, the
     // 56-register kernel (also 2% faster for the city pathtracer's waves).

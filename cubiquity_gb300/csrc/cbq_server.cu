@@ -293,7 +293,7 @@ cbq_status cbq_server::enqueue(Slot& s, const std::vector<Request*>& group)
         jd.q.compute_surface = rq->r.query.compute_surface;
         jd.q.max_footprint = rq->r.query.max_footprint;
         jd.q.flags = rq->r.query.flags;
-        if (!rq->r.dag->flat_ok) {  // coordinates beyond +-2^24: the nested kernel, launched on its own
+        if (!rq->r.dag->flat_ok) {  // integer positions (far coordinates, huge stores): launched on its own
             cbq_rays rays{o, d};
             cbq_hits hits{out.hit, out.distance, out.material, out.position, out.normal, out.voxel, out.status};
             cbq_status st = cbq_intersect(rq->r.dag, &rays, n, &rq->r.query, &hits, (cbq_stream_t)s.stream);

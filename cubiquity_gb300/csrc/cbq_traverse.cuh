@@ -93,8 +93,8 @@ __device__ __forceinline__ uint32_t load_child_compact(const uint32_t* __restric
     return __ldg(nodes + ((node >> 8) * 2u + __popc(m & ((1u << slot) - 1u))));  // offsets < 2^25 words
 }
 
-// WIDE: 64-bit word index (the nested kernel, any store size); otherwise the
-// store has fewer than 2^29 nodes.
+// WIDE: 64-bit word index (the nested and integer-position kernels, any store
+// size); otherwise the store has fewer than 2^29 nodes.
 template <bool COMPACT, bool WIDE = false>
 __device__ __forceinline__ uint32_t child_of(const uint32_t* __restrict__ nodes, uint32_t node, uint32_t slot,
                                              uint32_t& loads)

@@ -147,8 +147,9 @@ cbq_status cbq_dag_create(const uint32_t* host_nodes, uint64_t node_count, uint3
                           cbq_dag** out);
 /* cbq_dag_create with a device layout (CBQ_DAG_LAYOUT_*; no reference
  * counterpart).  COMPACT falls back to REFERENCE, with a log message, when the
- * DAG needs the nested kernel (coordinates beyond +-2^24) or the compact store
- * would exceed 128 MB; cbq_dag_get_info reports the layout in use. */
+ * DAG needs integer positions (coordinates beyond +-2^24, or 2^29 nodes or
+ * more) or the compact store would exceed 128 MB; cbq_dag_get_info reports the
+ * layout in use. */
 cbq_status cbq_dag_create_ex(const uint32_t* host_nodes, uint64_t node_count, uint32_t root,
                              uint32_t layout, cbq_dag** out);
 cbq_status cbq_dag_destroy(cbq_dag* dag);
@@ -157,9 +158,11 @@ cbq_status cbq_dag_get_info(const cbq_dag* dag, cbq_dag_info* info);
 /* Kernel selection and launch shape (chosen by the autotuner; 0 = default).
  *   CBQ_KERNEL_FLAT    one ray per thread, the ESVO loops flattened into one
  *                      per-lane state machine (lanes reconverge every step);
- *                      used when the DAG's coordinates lie within +-2^24
+ *                      child positions as exact floats where the DAG's
+ *                      coordinates lie within +-2^24 and it has fewer than
+ *                      2^29 nodes, else as wrapping i32 (any DAG); the default
  *   CBQ_KERNEL_NESTED  one ray per thread, the reference's nested loops as
- *                      written (any coordinates)
+ *                      written (any DAG; kept as a second restatement)
  * For cbq_intersect_persistent, `refill_min` (flat) is the number of idle lanes
  * at which a warp takes new rays and `chunk` (nested) the rays per warp grab. */
 typedef enum cbq_kernel {

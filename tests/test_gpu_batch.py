@@ -23,7 +23,7 @@ def small_batch():
         nodes, root = v.scene.build()
         o, d = v.make_rays()
         jobs.append((nodes, root, o, d))
-    # A volume far from the origin (nested kernel) and an empty batch.
+    # A volume far from the origin (integer positions: launched beside the batch kernel) and an empty batch.
     from conftest import relocate
     n2, r2 = relocate(jobs[0][0], jobs[0][1], vols[0].scene.edge_log2, (1 << 30, 0, 0))
     o2 = jobs[0][2].copy()
@@ -44,7 +44,8 @@ def test_batch_graph_and_direct_equal_single_volume_path(small_batch, orc):
     jobs, dags, dev = small_batch
     single = [cbq.intersect_volume(g, o, d) for g, (o, d) in zip(dags, dev)]
     batch = cbq.Batch([(g, o, d) for g, (o, d) in zip(dags, dev)])
-    assert batch.total_rays == sum(o.shape[0] for (o, _), g in zip(dev, dags) if g.launch_config()["kernel"] == 2)
+    # The far volume's rays (job 10) run beside the batch kernel, not in its ray count.
+    assert batch.total_rays == sum(o.shape[0] for o, _ in dev) - dev[10][0].shape[0]
     batch.launch()
     torch.cuda.synchronize()
     for j, (a, b) in enumerate(zip(batch.outputs, single)):

@@ -146,20 +146,28 @@ def test_persistent_equals_plain(terrain, kernel, chunk):
 @pytest.mark.parametrize("origin,flat", [((1 << 30, -(1 << 26), 3 << 20), False), ((3 << 20, 1 << 23, -(1 << 22)), True)])
 def test_relocated_volume(orc, origin, flat):
     """A volume far from the origin: beyond +-2^24 the float-position kernel
-    is not exact and the nested kernel is used; both agree with the oracle."""
+    is not exact and the flat kernel keeps integer positions instead; the
+    nested kernel, asked for, also agrees with the oracle."""
     from conftest import relocate
     nodes, root = W.SceneSpec(cbq.SCENE_SPHERES, 6, 11, 16).build()
     n2, r2 = relocate(nodes, root, 6, origin)
     cam = W.CameraSpec(tuple(np.add((-40.0, -40.0, 90.0), origin)), tuple(np.add((32.0, 32.0, 32.0), origin)), 48, 48)
     o, d = cam.rays()
     dag = cbq.Dag(n2, r2)
-    assert dag.launch_config()["kernel"] == (cbq.KERNEL_FLAT if flat else cbq.KERNEL_NESTED)
-    got = _host(cbq.intersect_volume(dag, _dev(o), _dev(d)))
+    assert dag.launch_config()["kernel"] == cbq.KERNEL_FLAT
     want = orc.intersect(n2, orc.find_subdags(n2, r2), o, d)
-    _assert_same(got, want, FIELDS + ("status",), what=f"relocated {origin}")
-    dag.set_launch_config(cbq.KERNEL_FLAT)  # requested, but only used where exact
+    for form in (cbq.FORM_PERSISTENT, cbq.FORM_PLAIN):
+        for stack in (cbq.STACK_LOCAL, cbq.STACK_SHARED):
+            dag.set_launch_config(cbq.KERNEL_FLAT, 64, 0, 8, stack, form, 8, 56)
+            got = _host(cbq.intersect_volume(dag, _dev(o), _dev(d)))
+            _assert_same(got, want, FIELDS + ("status",), what=f"relocated {origin} form {form} stack {stack}")
+    dag.set_launch_config(cbq.KERNEL_NESTED)
     got2 = _host(cbq.intersect_volume(dag, _dev(o), _dev(d)))
-    _assert_same(got2, want, FIELDS + ("status",), what=f"relocated {origin} flat requested")
+    _assert_same(got2, want, FIELDS + ("status",), what=f"relocated {origin} nested")
+    lod = orc.intersect(n2, orc.find_subdags(n2, r2), o, d, True, 0.05)
+    dag.set_launch_config()
+    got3 = _host(cbq.intersect_volume(dag, _dev(o), _dev(d), True, 0.05))
+    _assert_same(got3, lod, FIELDS + ("status",), what=f"relocated {origin} LOD")
 
 
 def test_host_api_equals_device_api(terrain):

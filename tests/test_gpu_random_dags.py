@@ -33,7 +33,7 @@ def test_random_dag_parity(seed, orc):
     rng = np.random.default_rng(1000 + seed)
     edge = 1 << int(rng.integers(2, 7))
     vox = random_voxels(rng, edge)
-    span = (1 << 30) if seed % 6 == 5 else (1 << 21)  # every sixth volume needs the nested kernel
+    span = (1 << 30) if seed % 6 == 5 else (1 << 21)  # every sixth volume needs integer positions
     origin = tuple(int(x) * edge for x in rng.integers(-span // edge, span // edge, 3))
     nodes, root = build_dag(vox, origin)
     o, d = random_rays(rng, origin, edge, 4000)
