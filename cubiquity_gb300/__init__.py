@@ -168,6 +168,7 @@ _sig("cbq_batch_set_launch_config", [_P, ctypes.POINTER(_BatchConfig)])
 _sig("cbq_batch_get_launch_config", [_P, ctypes.POINTER(_BatchConfig)])
 _sig("cbq_batch_autotune", [_P, _P, ctypes.c_int32])
 _sig("cbq_batch_launch", [_P, _P])
+_sig("cbq_batch_set_l2_persistence", [_P, _P, ctypes.c_float])
 _sig("cbq_batch_launch_direct", [_P, _P])
 _sig("cbq_batch_destroy", [_P])
 _sig("cbq_intersect_batch", [ctypes.POINTER(_Job), ctypes.c_int32, ctypes.POINTER(_Query), _P])
@@ -839,6 +840,12 @@ class Batch:
     def launch(self, stream=None) -> None:
         """Replays the captured CUDA graph (captured on first use)."""
         _check(_lib.cbq_batch_launch(self._h, _stream_ptr(stream)), "cbq_batch_launch")
+
+    def set_l2_persistence(self, dag: Dag | None, fraction: float) -> None:
+        """Persisting L2 window over `dag`'s node store on the graph's kernel
+        nodes (fraction of the device's persisting-L2 limit; 0 removes it)."""
+        _check(_lib.cbq_batch_set_l2_persistence(self._h, dag.handle if dag is not None else None, fraction),
+               "cbq_batch_set_l2_persistence")
 
     def launch_direct(self, stream=None) -> None:
         _check(_lib.cbq_batch_launch_direct(self._h, _stream_ptr(stream)), "cbq_batch_launch_direct")

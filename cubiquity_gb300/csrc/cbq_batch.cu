@@ -10,6 +10,7 @@
 #include "cbq_batch.cuh"
 
 #include <algorithm>
+#include <exception>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -307,6 +308,10 @@ struct cbq_batch {
     cbq_batch_config cfg{kBatchBlockDefault, kBatchRefillDefault, (int32_t)kBatchStepsDefault, 0, CBQ_STACK_LOCAL,
                          CBQ_FORM_PERSISTENT};
     cudaGraphExec_t exec = nullptr;
+    // Persisting L2 window set on the graph's kernel nodes (l2_bytes 0: none).
+    void* l2_base = nullptr;
+    size_t l2_bytes = 0;
+    float l2_hit_ratio = 0.0f;
 };
 
 namespace {
@@ -375,6 +380,36 @@ void drop_graph(cbq_batch* b)
     b->exec = nullptr;
 }
 
+// Sets the batch's persisting L2 window on every kernel node of the captured
+// graph (the traversal and, for sorted forms, the octant sort).
+cbq_status set_kernel_node_window(const cbq_batch* b, cudaGraph_t g)
+{
+    size_t count = 0;
+    if (cudaGraphGetNodes(g, nullptr, &count) != cudaSuccess) return CBQ_ERR_CUDA;
+    std::vector<cudaGraphNode_t> nodes;
+    try {
+        nodes.resize(count);
+    } catch (const std::exception&) {
+        return CBQ_ERR_OUT_OF_MEMORY;
+    }
+    if (count && cudaGraphGetNodes(g, nodes.data(), &count) != cudaSuccess) return CBQ_ERR_CUDA;
+    cudaKernelNodeAttrValue v;
+    std::memset(&v, 0, sizeof(v));
+    v.accessPolicyWindow.base_ptr = b->l2_base;
+    v.accessPolicyWindow.num_bytes = b->l2_bytes;
+    v.accessPolicyWindow.hitRatio = b->l2_hit_ratio;
+    v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    for (cudaGraphNode_t n : nodes) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(n, &t) != cudaSuccess) return CBQ_ERR_CUDA;
+        if (t != cudaGraphNodeTypeKernel) continue;
+        if (cudaGraphKernelNodeSetAttribute(n, cudaKernelNodeAttributeAccessPolicyWindow, &v) != cudaSuccess)
+            return CBQ_ERR_CUDA;
+    }
+    return CBQ_OK;
+}
+
 cbq_status capture_graph(cbq_batch* b)
 {
     drop_graph(b);
@@ -387,6 +422,7 @@ cbq_status capture_graph(cbq_batch* b)
         st = enqueue_batch(b, s);
         if (cudaStreamEndCapture(s, &g) != cudaSuccess) st = CBQ_ERR_CUDA;
     }
+    if (st == CBQ_OK && b->l2_bytes) st = set_kernel_node_window(b, g);
     if (st == CBQ_OK && cudaGraphInstantiate(&b->exec, g, 0) != cudaSuccess) st = CBQ_ERR_CUDA;
     if (g) cudaGraphDestroy(g);
     cudaStreamDestroy(s);
@@ -522,6 +558,33 @@ cbq_status cbq_batch_launch(cbq_batch* b, cbq_stream_t stream)
         if (st != CBQ_OK) return st;
     }
     return cudaGraphLaunch(b->exec, (cudaStream_t)stream) == cudaSuccess ? CBQ_OK : CBQ_ERR_CUDA;
+}
+
+cbq_status cbq_batch_set_l2_persistence(cbq_batch* b, const cbq_dag* dag, float fraction)
+{
+    if (!b || !(fraction >= 0.0f && fraction <= 1.0f)) return CBQ_ERR_INVALID_ARGUMENT;
+    if (fraction > 0.0f && (!dag || dag->device != b->device)) return CBQ_ERR_INVALID_ARGUMENT;
+    drop_graph(b);  // re-captured with the new window on the next cbq_batch_launch
+    if (fraction == 0.0f) {
+        b->l2_base = nullptr;
+        b->l2_bytes = 0;
+        // Give the set-aside back to normal caching and demote persisting lines
+        // (settings of the calling process's context).
+        if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0) != cudaSuccess ||
+            cudaCtxResetPersistingL2Cache() != cudaSuccess)
+            return CBQ_ERR_CUDA;
+        return CBQ_OK;
+    }
+    int max_window = 0, max_persist = 0;
+    cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, b->device);
+    cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, b->device);
+    if (max_window <= 0 || max_persist <= 0) return CBQ_OK;  // not supported: caching stays as it is
+    const size_t want = (size_t)((double)max_persist * fraction);
+    if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want) != cudaSuccess) return CBQ_ERR_CUDA;
+    b->l2_base = dag->d_nodes;
+    b->l2_bytes = std::min<size_t>(dag->device_bytes, (size_t)max_window);
+    b->l2_hit_ratio = (float)std::min(1.0, (double)want / (double)b->l2_bytes);
+    return CBQ_OK;
 }
 
 cbq_status cbq_batch_launch_direct(cbq_batch* b, cbq_stream_t stream)

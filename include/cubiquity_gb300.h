@@ -328,6 +328,14 @@ cbq_status cbq_batch_get_launch_config(const cbq_batch* b, cbq_batch_config* cfg
 cbq_status cbq_batch_autotune(cbq_batch* b, cbq_stream_t stream, int32_t repetitions);
 /* Replays the captured graph on `stream` (captures it first if needed). */
 cbq_status cbq_batch_launch(cbq_batch* b, cbq_stream_t stream);
+/* Pins one DAG's node store in L2 for the batch's graph launches: a persisting
+ * access-policy window over `dag`'s store, set on every kernel node of the
+ * graph (re-captured on the next cbq_batch_launch), reserving `fraction` of the
+ * device's persisting-L2 limit (a setting of the calling process's context);
+ * 0 removes the window, releases the set-aside and demotes persisting lines.
+ * Direct launches (cbq_batch_launch_direct) carry no window.  Measured on a
+ * 64-volume batch it does not help: the stores' L2 misses are first touches. */
+cbq_status cbq_batch_set_l2_persistence(cbq_batch* b, const cbq_dag* dag, float fraction);
 /* The same work launched directly, without the graph. */
 cbq_status cbq_batch_launch_direct(cbq_batch* b, cbq_stream_t stream);
 cbq_status cbq_batch_destroy(cbq_batch* b);

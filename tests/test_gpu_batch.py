@@ -193,3 +193,26 @@ def test_batch_lod_and_tmax_query(small_batch, stack, form):
             assert _eq(a[k], b[k]), f"job {j} {k}"
     assert any(int(r["hit"].sum()) > 0 for r in ref)
     batch.destroy()
+
+
+def test_batch_l2_window_on_the_graph_keeps_results(small_batch):
+    """A persisting L2 window over one job's node store, set on the graph's
+    kernel nodes, changes caching only: the results stay the same bits, and
+    removing it leaves the next launches unchanged too."""
+    jobs, dags, dev = small_batch
+    ref = [cbq.intersect_volume(g, o, d) for g, (o, d) in zip(dags, dev)]
+    batch = cbq.Batch([(g, o, d) for g, (o, d) in zip(dags, dev)])
+    big = max(range(len(dags) - 2), key=lambda i: dags[i].device_bytes)
+    for fraction in (1.0, 0.0):
+        batch.set_l2_persistence(dags[big] if fraction else None, fraction)
+        for out in batch.outputs:
+            for v in out.values():
+                v.fill_(0x3C)
+        batch.launch()
+        torch.cuda.synchronize()
+        for j, (a, b) in enumerate(zip(batch.outputs, ref)):
+            for k in FIELDS:
+                assert _eq(a[k], b[k]), f"job {j} {k} (window fraction {fraction})"
+    with pytest.raises(cbq.CbqError):
+        batch.set_l2_persistence(dags[0], 1.5)
+    batch.destroy()
