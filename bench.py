@@ -79,6 +79,11 @@ def parse_args():
                    help="terrain-4096: skip the batch-64 and serve-8 measurements added to the line")
     p.add_argument("--layout", choices=["reference", "compact"], default="reference",
                    help="device node store: the reference's array, or the compact store (occupied children only)")
+    p.add_argument("--node-order", choices=["builder", "bfs"], default="builder",
+                   help="batch-64: node stores as built, or renumbered breadth first (same results)")
+    p.add_argument("--l2-window", type=float, default=0.0,
+                   help="batch-64: persisting L2 window over the largest DAG on the batch graph's kernel nodes "
+                        "(fraction of the persisting-L2 limit; 0 = none)")
     p.add_argument("--serve-inflight", type=int, default=8, help="serve-8: launches in flight")
     p.add_argument("--serve-batch-rays", type=int, default=4 << 20, help="serve-8: rays per launch at most")
     p.add_argument("--serve-summary", action="store_true",
@@ -686,6 +691,8 @@ def measure_batch(args, world, local, e2e_steps: int | None = None):
 
     torch.cuda.set_device(local)
     host_jobs = batch_jobs()
+    if args.node_order == "bfs":  # the same graphs renumbered breadth first: same results
+        host_jobs = [cbq.reorder_bfs(n, r) + (o, d) for n, r, o, d in host_jobs]
     dags = [cbq.Dag(n, r, LAYOUTS[args.layout]) for n, r, _, _ in host_jobs]
     dev = [(torch.from_numpy(o).cuda(), torch.from_numpy(d).cuda()) for _, _, o, d in host_jobs]
     rays_per_step = sum(o.shape[0] for o, _ in dev)
@@ -693,6 +700,8 @@ def measure_batch(args, world, local, e2e_steps: int | None = None):
     plain_out = [cbq.alloc_hits(o.shape[0]) for o, _ in dev]
     batch = cbq.Batch([(g, o, d) for g, (o, d) in zip(dags, dev)])
     tuned = batch.autotune(3, stream=stream)
+    if args.l2_window > 0:  # persisting window over the largest store, on the graph's kernel nodes
+        batch.set_l2_persistence(max(dags, key=lambda g: g.device_bytes), args.l2_window)
     steps = max(3, args.steps)
 
     def plain_step():
@@ -836,6 +845,7 @@ def run_gpu_batch(args, world, rank, local):
         "config": {"workload": "batch-64", "volumes": s["volumes"], "rays_per_step": d["rays_per_step"],
                    "dag_bytes": d["dag_bytes"], "layout": args.layout, "device_node_bytes": d["device_node_bytes"],
                    "batch_config": d["tuned"], "form": "one persistent launch replayed from a CUDA graph",
+                   "node_order": args.node_order, "l2_window": args.l2_window,
                    "l2": "inputs larger than L2 (rays + hits %.0f MB per step)" % (d["rays_per_step"] * 78 / 1e6)},
         "plain": {"value": d["plain_value"], "unit": "Mrays/s", "ms_per_step": d["plain_ms"],
                   "form": "cbq_intersect once per volume (64 launches per step)"},
