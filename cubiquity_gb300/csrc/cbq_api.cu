@@ -284,7 +284,7 @@ cbq_status cbq_dag_create_ex(const uint32_t* host_nodes, uint64_t node_count, ui
             bytes = compact.size() * sizeof(uint32_t);
         } else {
             cbq::log(CBQ_LOG_WARNING, "compact layout unavailable (%s): using the reference layout",
-                     dag->flat_ok ? "store beyond 128 MB" : "coordinates beyond 2^24");
+                     dag->flat_ok ? "store beyond 128 MB" : "coordinates beyond 2^21");
         }
     }
     dag->device_bytes = bytes;
@@ -296,7 +296,7 @@ cbq_status cbq_dag_create_ex(const uint32_t* host_nodes, uint64_t node_count, ui
              "DAG uploaded to device %d: %llu nodes, %s layout (%.1f MB), root %u, max sub-DAG height %d, %s kernel",
              dag->device, (unsigned long long)node_count,
              dag->layout == CBQ_DAG_LAYOUT_COMPACT ? "compact" : "reference", bytes / 1e6, root, dag->max_height,
-             dag->flat_ok ? "flat (float positions)" : "flat (integer positions: coordinates beyond 2^24 or 2^29 nodes)");
+             dag->flat_ok ? "flat (float positions)" : "flat (integer positions: coordinates beyond 2^21 or 2^29 nodes)");
     *out = dag;
     return CBQ_OK;
 }

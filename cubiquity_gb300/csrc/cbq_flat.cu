@@ -143,15 +143,17 @@ __global__ void __launch_bounds__(256) cbq_k_octant_scatter(const float4* __rest
 }  // namespace dev
 
 // True when every occupied SubDAG's reflected coordinates stay within
-// +-2^24, so the flat kernel's float positions are exact, and the store has
-// fewer than 2^29 nodes, so its word offsets fit 32 bits.
+// +-2^21 (heights at most 21), so the flat kernel's float positions are exact
+// and their biased bit patterns carry the integer bits its pop reads, and the
+// store has fewer than 2^29 nodes, so its word offsets fit 32 bits.
 bool float_positions_exact(const cbq_dag* dag)
 {
     if (dag->node_count > dev::kFlatMaxNodes) return false;  // 32-bit node word offsets
-    const int64_t lim = (int64_t)1 << 24;
+    const int64_t lim = (int64_t)1 << 21;
     for (int i = 0; i < 8; i++) {
         const cbq_subdag& s = dag->subdags[i];
         if (s.node_index == 0) continue;
+        if (s.node_height > 21) return false;
         const int64_t size = (int64_t)1 << s.node_height;
         for (int a = 0; a < 3; a++) {
             const int64_t lo = s.lower_bound[a], hi = lo + size;
@@ -290,7 +292,7 @@ cbq_status launch_flat(const cbq_dag* dag, const dev::DagParams& dp, const dev::
     }
     if (dag->layout == CBQ_DAG_LAYOUT_COMPACT)
         return launch_ctx(make_ctx<dev::FlatCtxT<true>>(dp, q, out, orig, dir, nullptr), n, fl, rows, stream, dv);
-    if (!dag->flat_ok)  // coordinates beyond +-2^24 or 2^29 nodes or more: integer positions
+    if (!dag->flat_ok)  // coordinates beyond +-2^21 or 2^29 nodes or more: integer positions
         return launch_ctx(make_ctx<dev::FlatCtxT<false, false, true>>(dp, q, out, orig, dir, nullptr), n, fl, rows,
                           stream, dv);
     return launch_ctx(make_ctx<dev::FlatCtxT<false>>(dp, q, out, orig, dir, nullptr), n, fl, rows, stream, dv);

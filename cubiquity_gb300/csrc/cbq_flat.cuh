@@ -13,9 +13,10 @@
 // Floating-point operations are those of cbq_traverse.cuh / the reference, in
 // the same order (compile with -fmad=false).  Child positions are carried as
 // floats updated by exact float additions; the host only selects this form
-// when every SubDAG's reflected coordinates lie within +-2^24, where
-// (float)(a + b) == (float)a + (float)b, so the i32 positions the pop's
-// XOR/MSB logic needs are recovered exactly by conversion when a pop happens.
+// when every SubDAG's reflected coordinates lie within +-2^21, where
+// (float)(a + b) == (float)a + (float)b and p + 1.5 * 2^23 is exact with a
+// fixed exponent, so the integer bits the pop's XOR/MSB logic needs are the
+// low bits of that sum's bit pattern (no float/int conversion).
 #pragma once
 
 #include "../../include/cubiquity_gb300.h"
@@ -23,6 +24,10 @@
 
 namespace cbq {
 namespace dev {
+
+// Float positions p with |p| <= 2^21: the bit pattern of p + kPosBias is
+// 0x4B400000 + p (two's complement), exactly, so its low 22 bits are p's.
+constexpr float kPosBias = 12582912.0f;  // 1.5 * 2^23
 
 enum : uint32_t { kLaneIdle = 0u, kLaneEnter = 1u, kLaneNext = 2u, kLaneWalk = 3u };
 
@@ -33,7 +38,8 @@ struct Lane {
     float ddx, ddy, ddz;         // octant walk distances (distToOrigin)
     uint32_t sign, oct;
     // ESVO walk state
-    uint32_t node, cid, written;
+    uint32_t node, cid;
+    bool fresh;                  // walk not started: its descent stack is still to be cleared
     int32_t cns;
     float fx, fy, fz, fcns;      // child position and size as exact floats (float-position form)
     int32_t px, py, pz;          // child position as wrapping i32 (integer-position form)
@@ -59,7 +65,7 @@ struct FlatCtxT {
     static constexpr bool kCompact = COMPACT;
     // INT_POS: child positions as wrapping i32 converted to float where a slab
     // plane is needed (the reference's own arithmetic, any coordinates, 64-bit
-    // node offsets); otherwise exact floats (coordinates within +-2^24, fewer
+    // node offsets); otherwise exact floats (coordinates within +-2^21, fewer
     // than 2^29 nodes).
     static constexpr bool kIntPos = INT_POS;
     DagParams dag;
@@ -92,6 +98,22 @@ __device__ __forceinline__ uint32_t first_child_f(const Lane& L, float entry, fl
         id |= (L.rox >= fcx ? 1u : 0u) | (L.roy >= fcy ? 2u : 0u) | (L.roz >= fcz ? 4u : 0u);
     }
     return id;
+}
+
+// The same with each axis's bit also returned as a predicate, for callers that
+// move the child position by it (cheaper than unpacking the id again).
+__device__ __forceinline__ uint32_t first_child_p(const Lane& L, float entry, float fcx, float fcy, float fcz,
+                                                  bool& bx, bool& by, bool& bz)
+{
+    bx = ((fcx - L.rox) * L.ix) < entry;
+    by = ((fcy - L.roy) * L.iy) < entry;
+    bz = ((fcz - L.roz) * L.iz) < entry;
+    if (entry <= 0.0f) {
+        bx = bx || L.rox >= fcx;
+        by = by || L.roy >= fcy;
+        bz = bz || L.roz >= fcz;
+    }
+    return (uint32_t)bx | ((uint32_t)by << 1) | ((uint32_t)bz << 2);
 }
 
 // Per-ray set-up: intersectVolume up to the octant loop (raytracing.cpp:409-434).
@@ -227,7 +249,7 @@ __device__ __forceinline__ void lane_enter(Lane& L, const Src& c)
         L.fz = fpz + ((L.cid & 4u) ? L.fcns : 0.0f);
     }
     L.last_exit = exit_;
-    L.written = 0u;
+    L.fresh = true;
     L.mode = kLaneWalk;
 }
 
@@ -264,10 +286,7 @@ __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
         const float c0z = ((INT ? (float)L.pz : L.fz) - L.roz) * L.iz;
         const float tce = slab_max3<FAST>(c0x, c0y, c0z);
         if (child >= kMaterialCount && large_footprint(L.cns, tcx, c.query(L).max_footprint)) {
-            if (tcx < L.last_exit) {
-                stack.put(L.h, L.node);
-                L.written |= 1u << L.h;
-            }
+            if (tcx < L.last_exit) stack.put(L.h, L.node);
             L.last_exit = tcx;
             L.h--;
             L.node = child;
@@ -280,10 +299,12 @@ __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
                 if (L.cid & 4u) L.pz = wadd(L.pz, L.cns);
             } else {
                 L.fcns = (float)L.cns;
-                L.cid = first_child_f(L, tce, L.fx + L.fcns, L.fy + L.fcns, L.fz + L.fcns);
-                if (L.cid & 1u) L.fx += L.fcns;
-                if (L.cid & 2u) L.fy += L.fcns;
-                if (L.cid & 4u) L.fz += L.fcns;
+                const float mcx = L.fx + L.fcns, mcy = L.fy + L.fcns, mcz = L.fz + L.fcns;
+                bool bx, by, bz;
+                L.cid = first_child_p(L, tce, mcx, mcy, mcz, bx, by, bz);
+                L.fx = bx ? mcx : L.fx;
+                L.fy = by ? mcy : L.fy;
+                L.fz = bz ? mcz : L.fz;
             }
         } else {
             uint32_t material = 0u;
@@ -303,33 +324,46 @@ __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
         }
         return;
     }
-    const uint32_t flips = (c1x <= tcx ? 1u : 0u) | (c1y <= tcx ? 2u : 0u) | (c1z <= tcx ? 4u : 0u);
-    if (flips == 0u) {
+    const bool ax = c1x <= tcx, ay = c1y <= tcx, az = c1z <= tcx;
+    const uint32_t flips = (uint32_t)ax | ((uint32_t)ay << 1) | ((uint32_t)az << 2);
+    // With slab distances that cannot be NaN (FAST), tcx is one of the three
+    // and that axis flips: only the reference's form can get stuck here.
+    if (!FAST && !(ax || ay || az)) {
         L.status = kRayStuck;
         lane_finish(L, c, false, 0.0f, 0u, 0.0f, 0.0f, 0.0f);
         return;
     }
     L.cid ^= flips;
+    float ofx = 0.0f, ofy = 0.0f, ofz = 0.0f;  // float positions before the advance
     if constexpr (INT) {
-        if (flips & 1u) L.px = wadd(L.px, L.cns);
-        if (flips & 2u) L.py = wadd(L.py, L.cns);
-        if (flips & 4u) L.pz = wadd(L.pz, L.cns);
+        if (ax) L.px = wadd(L.px, L.cns);
+        if (ay) L.py = wadd(L.py, L.cns);
+        if (az) L.pz = wadd(L.pz, L.cns);
     } else {
-        if (flips & 1u) L.fx += L.fcns;
-        if (flips & 2u) L.fy += L.fcns;
-        if (flips & 4u) L.fz += L.fcns;
+        ofx = L.fx;
+        ofy = L.fy;
+        ofz = L.fz;
+        if (ax) L.fx += L.fcns;
+        if (ay) L.fy += L.fcns;
+        if (az) L.fz += L.fcns;
     }
     if ((L.cid & flips) != flips) {
-        // Integer positions: the wrapping i32 ones, or from the exact float ones
-        // (|p| < 2^24).  On a flipped axis the position before the advance was
-        // p - childSize.
-        const int32_t cx = INT ? L.px : __float2int_rz(L.fx);
-        const int32_t cy = INT ? L.py : __float2int_rz(L.fy);
-        const int32_t cz = INT ? L.pz : __float2int_rz(L.fz);
-        const uint32_t cs = (uint32_t)L.cns;
-        const uint32_t diff = ((flips & 1u) ? ((uint32_t)cx ^ ((uint32_t)cx - cs)) : 0u) |
-                              ((flips & 2u) ? ((uint32_t)cy ^ ((uint32_t)cy - cs)) : 0u) |
-                              ((flips & 4u) ? ((uint32_t)cz ^ ((uint32_t)cz - cs)) : 0u);
+        // The pop (raytracing.cpp:339-361) on integer positions: the wrapping
+        // i32 ones, or the biased bit patterns of the float ones, whose low 22
+        // bits are the integer's.  The highest differing bit is the same in
+        // both below bit 21; at bit 21 or above (a sign change included) both
+        // leave the SubDAG, whose height is at most 21.
+        const uint32_t cx = INT ? (uint32_t)L.px : __float_as_uint(L.fx + kPosBias);
+        const uint32_t cy = INT ? (uint32_t)L.py : __float_as_uint(L.fy + kPosBias);
+        const uint32_t cz = INT ? (uint32_t)L.pz : __float_as_uint(L.fz + kPosBias);
+        uint32_t diff;
+        if constexpr (INT) {  // on a flipped axis the position before the advance was p - childSize
+            const uint32_t cs = (uint32_t)L.cns;
+            diff = (ax ? (cx ^ (cx - cs)) : 0u) | (ay ? (cy ^ (cy - cs)) : 0u) | (az ? (cz ^ (cz - cs)) : 0u);
+        } else {  // before against after: an axis that did not move gives 0
+            diff = (cx ^ __float_as_uint(ofx + kPosBias)) | (cy ^ __float_as_uint(ofy + kPosBias)) |
+                   (cz ^ __float_as_uint(ofz + kPosBias));
+        }
         const int msb = 31 - __clz(diff);
         const int h = msb + 1;
         if (h > L.start_h) {  // left the sub-DAG: on to the next octant
@@ -337,20 +371,22 @@ __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
             return;
         }
         L.h = h;
-        L.node = (L.written & (1u << h)) ? stack.get(h) : 0u;
+        L.node = stack.get(h);
         L.cns = (int32_t)(1u << msb);
-        L.cid = (((uint32_t)cx >> msb) & 1u) | ((((uint32_t)cy >> msb) & 1u) << 1) |
-                ((((uint32_t)cz >> msb) & 1u) << 2);
         const uint32_t keep = 0u - (uint32_t)L.cns;
         if constexpr (INT) {
-            L.px = (int32_t)((uint32_t)cx & keep);
-            L.py = (int32_t)((uint32_t)cy & keep);
-            L.pz = (int32_t)((uint32_t)cz & keep);
+            L.cid = ((cx >> msb) & 1u) | (((cy >> msb) & 1u) << 1) | (((cz >> msb) & 1u) << 2);
+            L.px = (int32_t)(cx & keep);
+            L.py = (int32_t)(cy & keep);
+            L.pz = (int32_t)(cz & keep);
         } else {
-            L.fcns = (float)L.cns;
-            L.fx = (float)(int32_t)((uint32_t)cx & keep);
-            L.fy = (float)(int32_t)((uint32_t)cy & keep);
-            L.fz = (float)(int32_t)((uint32_t)cz & keep);
+            // Bit msb (< 21) of each axis, gathered at msb..msb+2, then shifted down.
+            const uint32_t m = (uint32_t)L.cns;
+            L.cid = ((cx & m) + ((cy & m) << 1) + ((cz & m) << 2)) >> msb;
+            L.fcns = __uint_as_float((uint32_t)(127 + msb) << 23);  // 2^msb
+            L.fx = __uint_as_float(cx & keep) - kPosBias;
+            L.fy = __uint_as_float(cy & keep) - kPosBias;
+            L.fz = __uint_as_float(cz & keep) - kPosBias;
         }
         L.last_exit = 0.0f;
     }
@@ -364,6 +400,10 @@ template <bool FAST, typename Src, typename Stack>
 __device__ __forceinline__ void lane_walk_steps(Lane& L, const Src& c, Stack& stack, uint32_t steps)
 {
     if (L.mode != kLaneWalk) return;
+    if (L.fresh) {  // each SubDAG walk starts on a zeroed stack (never-written slots read as node 0)
+        stack.clear(L.start_h);
+        L.fresh = false;
+    }
     const uint32_t budget = kMaxFetches - L.fetches;  // > 0: a walking lane is below the cap
     // Every step makes one fetch, so the fetch count doubles as the step counter.
     const uint32_t end = L.fetches + (steps < budget ? steps : budget);

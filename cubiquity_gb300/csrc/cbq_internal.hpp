@@ -86,7 +86,7 @@ struct cbq_dag {
     cbq_subdag subdags[8];
     int32_t max_height = 0;        // max SubDAG height (stack depth)
     int device = 0;
-    bool flat_ok = false;          // float-position flat kernel applies (coordinates within +-2^24,
+    bool flat_ok = false;          // float-position flat kernel applies (coordinates within +-2^21,
                                    // under 2^29 nodes); otherwise the integer-position form
     // Defaults from the GB300 sweep on terrain-4096 (primary and bounce rays):
     // persistent refill, stack in local memory, 8 ESVO steps per loop iteration, the

@@ -65,24 +65,32 @@ extern "C" cbq_status cbq_measure_l2(uint64_t working_set_bytes, int iterations,
     cudaEventCreate(&a);
     cudaEventCreate(&b);
     const int grid = sms * 8;
-    // Warm the L2 with one pass, then time `iterations` passes.
+    // Each probe: one untimed pass (warms the L2), then the fastest of three
+    // timed launches (a GPU just out of idle may still be raising its clocks).
+    constexpr int kTimed = 3;
+    float ms = 0, best = 0;
     cbq_k_l2_stream<<<grid, 256>>>((const uint4*)buf, ws / 16, 1, sink);
-    cudaEventRecord(a);
-    cbq_k_l2_stream<<<grid, 256>>>((const uint4*)buf, ws / 16, iterations, sink);
-    cudaEventRecord(b);
-    cudaEventSynchronize(b);
-    float ms = 0;
-    cudaEventElapsedTime(&ms, a, b);
-    *stream_gbs = (double)ws * iterations / (ms * 1e-3) / 1e9;
+    for (int r = 0; r < kTimed; r++) {
+        cudaEventRecord(a);
+        cbq_k_l2_stream<<<grid, 256>>>((const uint4*)buf, ws / 16, iterations, sink);
+        cudaEventRecord(b);
+        cudaEventSynchronize(b);
+        cudaEventElapsedTime(&ms, a, b);
+        best = r == 0 ? ms : std::min(best, ms);
+    }
+    *stream_gbs = (double)ws * iterations / (best * 1e-3) / 1e9;
     const int rand_iters = 64;
     cbq_k_l2_random<<<grid, 256>>>((const uint32_t*)buf, (uint32_t)(ws / 4 - 1), 4, sink);
-    cudaEventRecord(a);
-    cbq_k_l2_random<<<grid, 256>>>((const uint32_t*)buf, (uint32_t)(ws / 4 - 1), rand_iters, sink);
-    cudaEventRecord(b);
-    cudaEventSynchronize(b);
-    cudaEventElapsedTime(&ms, a, b);
+    for (int r = 0; r < kTimed; r++) {
+        cudaEventRecord(a);
+        cbq_k_l2_random<<<grid, 256>>>((const uint32_t*)buf, (uint32_t)(ws / 4 - 1), rand_iters, sink);
+        cudaEventRecord(b);
+        cudaEventSynchronize(b);
+        cudaEventElapsedTime(&ms, a, b);
+        best = r == 0 ? ms : std::min(best, ms);
+    }
     const double loads = (double)grid * 256 * rand_iters * 8;
-    *random_gsectors_per_s = loads / (ms * 1e-3) / 1e9;
+    *random_gsectors_per_s = loads / (best * 1e-3) / 1e9;
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     cudaFree(buf);

@@ -139,9 +139,15 @@ __device__ __forceinline__ bool large_footprint(int32_t cns, float t_exit, float
 
 // Stack held in a per-thread local array (L1-resident).
 struct LocalStack {
-    uint32_t slot[32];
+    alignas(16) uint32_t slot[32];
     __device__ __forceinline__ void put(int h, uint32_t v) { slot[h & 31] = v; }
     __device__ __forceinline__ uint32_t get(int h) const { return slot[h & 31]; }
+    // Zeroes every slot (eight 16-byte stores); `top` is for the shared form.
+    __device__ __forceinline__ void clear(int /*top*/)
+    {
+#pragma unroll
+        for (int i = 0; i < 8; i++) reinterpret_cast<uint4*>(slot)[i] = make_uint4(0u, 0u, 0u, 0u);
+    }
 };
 
 // Stack held in shared memory, one column per thread: slot h at
@@ -151,6 +157,11 @@ struct SharedStack {
     uint32_t stride;
     __device__ __forceinline__ void put(int h, uint32_t v) { base[(uint32_t)(h - 1) * stride] = v; }
     __device__ __forceinline__ uint32_t get(int h) const { return base[(uint32_t)(h - 1) * stride]; }
+    // Zeroes slots 1..top.
+    __device__ __forceinline__ void clear(int top)
+    {
+        for (int h = 1; h <= top; h++) put(h, 0u);
+    }
 };
 
 struct EsvoOut {

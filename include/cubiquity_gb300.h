@@ -147,7 +147,7 @@ cbq_status cbq_dag_create(const uint32_t* host_nodes, uint64_t node_count, uint3
                           cbq_dag** out);
 /* cbq_dag_create with a device layout (CBQ_DAG_LAYOUT_*; no reference
  * counterpart).  COMPACT falls back to REFERENCE, with a log message, when the
- * DAG needs integer positions (coordinates beyond +-2^24, or 2^29 nodes or
+ * DAG needs integer positions (coordinates beyond +-2^21, or 2^29 nodes or
  * more) or the compact store would exceed 128 MB; cbq_dag_get_info reports the
  * layout in use. */
 cbq_status cbq_dag_create_ex(const uint32_t* host_nodes, uint64_t node_count, uint32_t root,
@@ -159,7 +159,7 @@ cbq_status cbq_dag_get_info(const cbq_dag* dag, cbq_dag_info* info);
  *   CBQ_KERNEL_FLAT    one ray per thread, the ESVO loops flattened into one
  *                      per-lane state machine (lanes reconverge every step);
  *                      child positions as exact floats where the DAG's
- *                      coordinates lie within +-2^24 and it has fewer than
+ *                      coordinates lie within +-2^21 and it has fewer than
  *                      2^29 nodes, else as wrapping i32 (any DAG); the default
  *   CBQ_KERNEL_NESTED  one ray per thread, the reference's nested loops as
  *                      written (any DAG; kept as a second restatement)
@@ -491,8 +491,9 @@ cbq_status cbq_count_fetches(const cbq_dag* dag, const cbq_rays* rays, uint64_t 
 /* Diagnostic (no reference counterpart): on the current device, measures the
  * streaming read bandwidth of an L2-resident buffer of about working_set_bytes
  * (GB/s) and the rate of independent random 32-byte-sector reads within it
- * (Gsectors/s).  These are the roofline denominators of the traversal, whose
- * node fetches are L2 sectors.  Synchronous. */
+ * (Gsectors/s), each the fastest of three timed launches after a warm-up pass.
+ * These are the roofline denominators of the traversal, whose node fetches are
+ * L2 sectors.  Synchronous. */
 cbq_status cbq_measure_l2(uint64_t working_set_bytes, int iterations, double* stream_gbs,
                           double* random_gsectors_per_s);
 

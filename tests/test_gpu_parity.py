@@ -143,16 +143,25 @@ def test_persistent_equals_plain(terrain, kernel, chunk):
     _assert_same(c, a, FIELDS + ("status",), what=f"plain {kernel}")
 
 
-@pytest.mark.parametrize("origin,flat", [((1 << 30, -(1 << 26), 3 << 20), False), ((3 << 20, 1 << 23, -(1 << 22)), True)])
+@pytest.mark.parametrize("origin,flat", [((1 << 30, -(1 << 26), 3 << 20), False),
+                                         ((3 << 20, 1 << 23, -(1 << 22)), False),
+                                         (((1 << 21) - 64, -(1 << 21), 5 << 18), True),
+                                         ((1 << 21, 0, 0), False)])
 def test_relocated_volume(orc, origin, flat):
-    """A volume far from the origin: beyond +-2^24 the float-position kernel
-    is not exact and the flat kernel keeps integer positions instead; the
-    nested kernel, asked for, also agrees with the oracle."""
+    """A volume away from the origin: the float-position kernel applies while
+    every SubDAG lies within +-2^21 (flat=True: its box touches 2^21 and -2^21);
+    beyond, the flat kernel keeps integer positions instead.  The nested
+    kernel, asked for, also agrees with the oracle."""
     from conftest import relocate
     nodes, root = W.SceneSpec(cbq.SCENE_SPHERES, 6, 11, 16).build()
     n2, r2 = relocate(nodes, root, 6, origin)
     cam = W.CameraSpec(tuple(np.add((-40.0, -40.0, 90.0), origin)), tuple(np.add((32.0, 32.0, 32.0), origin)), 48, 48)
     o, d = cam.rays()
+    # The compact layout needs the float-position form: which layout the DAG
+    # gets shows which form applies.
+    probe = cbq.Dag(n2, r2, cbq.LAYOUT_COMPACT)
+    assert probe.layout == (cbq.LAYOUT_COMPACT if flat else cbq.LAYOUT_REFERENCE)
+    probe.destroy()
     dag = cbq.Dag(n2, r2)
     assert dag.launch_config()["kernel"] == cbq.KERNEL_FLAT
     want = orc.intersect(n2, orc.find_subdags(n2, r2), o, d)
