@@ -47,6 +47,7 @@ struct Lane {
     float last_exit;
     uint32_t fetches, status, mode;
     bool fast;                   // no slab distance can be NaN or -0: min/max need no NaN ordering
+    bool pending;                // finished in this step batch, result held in node/last_exit/cid
     uint32_t loads;              // node loads made (fetches minus skipped empty children)
     uint32_t job;                // batch kernel: index of the lane's job
     uint64_t ray;                // ray index within its job
@@ -185,6 +186,41 @@ __device__ __forceinline__ void lane_finish(Lane& L, const Src& c, bool hit, flo
     L.mode = kLaneIdle;
 }
 
+// A finish inside the step loop.  The result is held in walk state that is
+// dead once the ray is done (node: hit | status << 8 | entry-plane bits << 16
+// | surface << 19; last_exit: distance; cid: material) and written by
+// flush_held after the step batch, by all the warp's lanes that finished in
+// it at once: finishes are spread over the steps, so writing each at once ran
+// the result code (position, normal, thirteen stores) at a few active lanes.
+__device__ __forceinline__ void lane_hold(Lane& L, bool hit, float dist, uint32_t material, uint32_t planes,
+                                          bool surface)
+{
+    L.node = (hit ? 1u : 0u) | (L.status << 8) | (planes << 16) | (surface ? (1u << 19) : 0u);
+    L.last_exit = dist;
+    L.cid = material;
+    L.pending = true;
+    L.mode = kLaneIdle;
+}
+
+// Writes a held result: the normal is the reference's
+// vec3(equal(tChildEntry, childT0)) * -rayDirSign (raytracing.cpp:314-315),
+// from the held plane bits.
+template <typename Src>
+__device__ __forceinline__ void flush_held(Lane& L, const Src& c)
+{
+    if (!L.pending) return;
+    L.pending = false;
+    const uint32_t w = L.node;
+    float nx = 0.0f, ny = 0.0f, nz = 0.0f;
+    if (w & (1u << 19)) {
+        nx = __fmul_rn((w & (1u << 16)) ? 1.0f : 0.0f, (L.sign & 1u) ? 1.0f : -1.0f);
+        ny = __fmul_rn((w & (1u << 17)) ? 1.0f : 0.0f, (L.sign & 2u) ? 1.0f : -1.0f);
+        nz = __fmul_rn((w & (1u << 18)) ? 1.0f : 0.0f, (L.sign & 4u) ? 1.0f : -1.0f);
+    }
+    L.status = (w >> 8) & 0xffu;
+    lane_finish(L, c, w & 1u, L.last_exit, L.cid, nx, ny, nz);
+}
+
 // One octant transition (raytracing.cpp:469-475).
 template <typename Src>
 __device__ __forceinline__ void lane_next(Lane& L, const Src& c)
@@ -307,20 +343,18 @@ __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
                 L.fz = bz ? mcz : L.fz;
             }
         } else {
-            uint32_t material = 0u;
-            float nx = 0.0f, ny = 0.0f, nz = 0.0f;
-            if (c.query(L).compute_surface) {
+            uint32_t material = 0u, planes = 0u;
+            const bool surface = c.query(L).compute_surface;
+            if (surface) {
                 material = nearest_material<Src::kCompact, INT>(c.nodes(L), child, L.sign, L.fetches, L.status,
                                                                 L.loads);
                 if (L.status != kRayOk) {
-                    lane_finish(L, c, false, 0.0f, 0u, 0.0f, 0.0f, 0.0f);
+                    lane_hold(L, false, 0.0f, 0u, 0u, false);
                     return;
                 }
-                nx = __fmul_rn(tce == c0x ? 1.0f : 0.0f, (L.sign & 1u) ? 1.0f : -1.0f);
-                ny = __fmul_rn(tce == c0y ? 1.0f : 0.0f, (L.sign & 2u) ? 1.0f : -1.0f);
-                nz = __fmul_rn(tce == c0z ? 1.0f : 0.0f, (L.sign & 4u) ? 1.0f : -1.0f);
+                planes = (tce == c0x ? 1u : 0u) | (tce == c0y ? 2u : 0u) | (tce == c0z ? 4u : 0u);
             }
-            lane_finish(L, c, true, tce, material, nx, ny, nz);
+            lane_hold(L, true, tce, material, planes, surface);
         }
         return;
     }
@@ -330,7 +364,7 @@ __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
     // and that axis flips: only the reference's form can get stuck here.
     if (!FAST && !(ax || ay || az)) {
         L.status = kRayStuck;
-        lane_finish(L, c, false, 0.0f, 0u, 0.0f, 0.0f, 0.0f);
+        lane_hold(L, false, 0.0f, 0u, 0u, false);
         return;
     }
     L.cid ^= flips;
@@ -410,12 +444,13 @@ __device__ __forceinline__ void lane_walk_steps(Lane& L, const Src& c, Stack& st
     while (L.fetches < end && L.mode == kLaneWalk) lane_walk<FAST>(L, c, stack);
     if (L.mode == kLaneWalk && L.fetches >= kMaxFetches) {
         L.status = kRayIterLimit;
-        lane_finish(L, c, false, 0.0f, 0u, 0.0f, 0.0f, 0.0f);
+        lane_hold(L, false, 0.0f, 0u, 0u, false);
     }
 }
 
 // The walk of a whole warp (all 32 lanes must call it): the FAST min/max when
-// every walking lane's ray allows it, else the reference's forms.
+// every walking lane's ray allows it, else the reference's forms; then the
+// results of the rays that finished in it are written.
 template <typename Src, typename Stack>
 __device__ __forceinline__ void warp_walk_steps(Lane& L, const Src& c, Stack& stack, uint32_t steps)
 {
@@ -423,6 +458,7 @@ __device__ __forceinline__ void warp_walk_steps(Lane& L, const Src& c, Stack& st
         lane_walk_steps<true>(L, c, stack, steps);
     else
         lane_walk_steps<false>(L, c, stack, steps);
+    flush_held(L, c);
 }
 
 // Octant transitions until the lane walks a SubDAG or has finished.  Bounded:
