@@ -484,20 +484,23 @@ def run_gpu(args, world, rank, local):
         label, po, pd, outs = item
         cbq.intersect_volume_host(e2e_dags[label], po, pd, out=outs)
 
-    # The batches are independent streams of work, so a caller issues each from
-    # its own host thread: thread b makes batch b's call once per step, and the
-    # calls of different batches overlap their copies and traversals (the host
-    # entry point is thread-safe).  The clock runs from the start until every
-    # thread has made its e2e_steps calls, i.e. every step's rays were copied in
-    # and its hits copied out.  The single-thread figure (the batches' calls one
+    # The batches are independent streams of work, so a caller issues them from
+    # one host thread per batch, and the calls of different threads overlap
+    # their copies and traversals (the host entry point is thread-safe).  The
+    # threads alternate the batches (thread t's k-th call is batch (t + k) mod
+    # the number of batches), so each makes one call of every batch per round of
+    # calls and no thread is left running alone at the end; over all threads
+    # each batch is called e2e_steps times.  The clock runs from the start until
+    # every thread has made its calls, i.e. every step's rays were copied in and
+    # its hits copied out.  The single-thread figure (the batches' calls one
     # after the other) is kept beside it.
     def e2e_timed(threaded: bool) -> float:
         errors = []
 
-        def worker(h):
+        def worker(t):
             try:
-                for _ in range(args.e2e_steps):
-                    e2e_call(h)
+                for k in range(args.e2e_steps):
+                    e2e_call(host[(t + k) % len(host)])
             except Exception as e:  # noqa: BLE001  (re-raised below: a failed call voids the figure)
                 errors.append(e)
         for h in host:  # warm-up: staging sets allocated
@@ -505,7 +508,7 @@ def run_gpu(args, world, rank, local):
         barrier(world)
         t = time.perf_counter()
         if threaded:
-            th = [threading.Thread(target=worker, args=(h,)) for h in host]
+            th = [threading.Thread(target=worker, args=(t,)) for t in range(len(host))]
             for x in th:
                 x.start()
             for x in th:
@@ -554,7 +557,7 @@ def run_gpu(args, world, rank, local):
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": rays_per_step * RAY_BYTES,
                 "d2h_bytes_per_step": rays_per_step * REF_HIT_BYTES,
                 "api": "cbq_intersect_host (pinned host buffers, copies pipelined with the traversal inside), "
-                       "one call per batch and step, each batch's calls from its own host thread (%d)" % len(host),
+                       "one call per batch and step, from %d host threads that alternate the batches" % len(host),
                 "fields": "hit, distance, material, position, normal (the reference's RayVolumeIntersection)",
                 "steps": args.e2e_steps, "one_thread_value": e2e_one_thread},
         "gpu_launches": launches,
@@ -997,6 +1000,16 @@ def measure_serve(args, world, local, half_runs: int = 3, half_seconds: float = 
         "arrivals": "open-loop Poisson, replayed by the library's native driver (cbq_server_replay)",
         "buffers": buffers, "clocks": clk,
     }
+    # The generator's threads spin through the last 200 us before each arrival,
+    # so their lateness measures how late the host ran this process's threads;
+    # the server's threads wait the same way, so a late host delays completions
+    # alike and the p99 then describes the host, not the server.
+    late_p99 = half["generator_lateness_ms"]["p99"]
+    summary["host_threads_stalled"] = bool(late_p99 > 0.2)
+    if late_p99 > 0.2:
+        summary["host_note"] = ("the load generator's own threads were late by p99 %.2f ms: the host did not run this "
+                                "process's threads on time (measured on these hosts for minutes after another "
+                                "process freed device memory)" % late_p99)
     details = {"scenes": scenes, "in_place": in_place, "peak": peak, "peak_rps": peak_rps, "other": other,
                "half": half, "sweep": sweep_runs, "clk": clk, "buffers": buffers}
     return summary, details

@@ -54,8 +54,11 @@ cbq_status noalloc_prepare(int device);
 constexpr int kHostStagesMax = 4;
 
 // cbq_intersect_host splits a call into at most kHostChunksMax chunks of at
-// least kHostChunkMin rays.
+// least kHostChunkMin rays; kHostChunksConcurrent while another call is in
+// flight in the process (its copies and traversals fill the gaps that smaller
+// chunks would, so fewer persistent-launch tails pay more).
 constexpr uint64_t kHostChunksMax = 8;
+constexpr uint64_t kHostChunksConcurrent = 4;
 constexpr uint64_t kHostChunkMin = 1ull << 18;
 // ... each made of about kHostBlocksPerChunk blocks of consecutive rays (at least
 // kHostBlockMin) dealt round-robin.
