@@ -206,9 +206,12 @@ def profiled_figure(workload: str, name: str, label: str | None = None):
     f = ROOT / "profiles" / f"traverse_{workload}.md"
     if not f.exists():
         return None
-    key = re.escape(name) + (r"\[" + re.escape(label) + r"\]" if label else "")
-    m = re.search(r"^" + key + r":\s*([0-9.]+)", f.read_text(), re.M)
-    return float(m.group(1)) if m else None
+    text = f.read_text()
+    for key in ([re.escape(name) + r"\[" + re.escape(label) + r"\]"] if label else []) + [re.escape(name)]:
+        m = re.search(r"^" + key + r":\s*([0-9.]+)", text, re.M)
+        if m:  # the batch's own figure, else the workload's (one-batch workloads)
+            return float(m.group(1))
+    return None
 
 
 def dist_setup(args):
@@ -556,8 +559,9 @@ def run_gpu(args, world, rank, local):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": rays_per_step * RAY_BYTES,
                 "d2h_bytes_per_step": rays_per_step * REF_HIT_BYTES,
-                "api": "cbq_intersect_host (pinned host buffers, copies pipelined with the traversal inside), "
-                       "one call per batch and step, from %d host threads that alternate the batches" % len(host),
+                "api": "cbq_intersect_host (pinned host buffers, copies pipelined with the traversal inside), " +
+                       ("one call per batch and step, from %d host threads that alternate the batches" % len(host)
+                        if len(host) > 1 else "one call per step"),
                 "fields": "hit, distance, material, position, normal (the reference's RayVolumeIntersection)",
                 "steps": args.e2e_steps, "one_thread_value": e2e_one_thread},
         "gpu_launches": launches,

@@ -396,8 +396,8 @@ class Dag:
             pass
 
     def set_launch_config(self, kernel: int = KERNEL_AUTO, block: int = 0, chunk: int = 0,
-                          refill_min: int = 0, stack: int = STACK_LOCAL, form: int = FORM_PERSISTENT,
-                          steps: int = 8, registers: int = 56) -> None:
+                          refill_min: int = 0, stack: int = STACK_SHARED, form: int = FORM_PERSISTENT,
+                          steps: int = 16, registers: int = 0) -> None:
         cfg = LaunchConfig(kernel, block, chunk, refill_min, stack, form, steps, registers)
         _check(_lib.cbq_dag_set_launch_config(self.handle, ctypes.byref(cfg)), "cbq_dag_set_launch_config")
 

@@ -16,7 +16,7 @@ using namespace cbq;
 
 namespace {
 
-constexpr int kFlatBlockDefault = 64;  // GB300, terrain-4096: 64, 128 and 256 threads within 1%
+constexpr int kFlatBlockDefault = 128;  // GB300, terrain-4096: 64, 128 and 256 threads within 1-3%
 constexpr uint32_t kRefillDefault = 8;
 
 bool use_flat(const cbq_dag* dag)

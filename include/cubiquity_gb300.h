@@ -183,10 +183,11 @@ typedef struct cbq_launch_config {
     int32_t block;            /* threads per block (multiple of 32, <= 256), 0 = default */
     uint32_t chunk;           /* nested persistent: rays per warp grab, 0 = default */
     uint32_t refill_min;      /* flat persistent: idle lanes that trigger a refill, 0 = default */
-    int32_t stack;            /* CBQ_STACK_* (flat kernel) */
+    int32_t stack;            /* CBQ_STACK_* (flat kernel; shared by default) */
     int32_t form;             /* CBQ_FORM_*, used by cbq_intersect_auto */
-    int32_t steps;            /* flat kernel: ESVO steps per loop iteration (1..32), 0 = 1 */
-    int32_t registers;        /* 0, or 56 (the default): the persistent local-stack
+    int32_t steps;            /* flat kernel: ESVO steps per loop iteration (1..32, 16 by
+                                 default), 0 = 1 */
+    int32_t registers;        /* 0 (the default), or 56: the persistent local-stack
                                  kernel held to 56 registers per thread (more
                                  resident warps); other forms ignore it */
 } cbq_launch_config;

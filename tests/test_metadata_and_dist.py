@@ -104,3 +104,15 @@ def test_reference_arm_under_torchrun_two_ranks():
     cb = j["cpu_baseline"]
     assert cb["value"] == j["value"] and cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["sample"]
     assert j["e2e"] == {"value": j["value"], "unit": j["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+@pytest.mark.parametrize("script", ["bench.py", "__graft_entry__.py"])
+def test_entry_scripts_compile_without_warnings(script):
+    """The bench and the entry module compile with warnings as errors (a
+    SyntaxWarning such as a string literal followed by a parenthesised
+    expression is a call that fails only when the line runs)."""
+    import warnings
+    src = (ROOT / script).read_text()
+    with warnings.catch_warnings():
+        warnings.simplefilter("error")
+        compile(src, script, "exec")
