@@ -1044,7 +1044,10 @@ def run_gpu_serve(args, world, rank, local):
         "half_load": half, "sweep": d["sweep"],
         "e2e": {"value": half["mrays_per_s"], "unit": "Mrays/s", "note": "host rays in, host hits out, per request"},
         "gpu_launches": half["launches"], "clocks": d["clk"],
+        "host_threads_stalled": s["host_threads_stalled"],
     }
+    if "host_note" in s:
+        line["host_note"] = s["host_note"]
     if rank == 0:
         print(json.dumps(line), flush=True)
 
