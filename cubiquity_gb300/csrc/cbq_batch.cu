@@ -74,7 +74,7 @@ __device__ __forceinline__ void batch_body(const JobDesc* __restrict__ jobs, uin
     const uint32_t below = (1u << lane) - 1u;
     Lane L;
     L.mode = kLaneIdle;
-    L.pending = false;
+    L.held = 0u;
     L.job = 0;
     L.nodes = nullptr;
     bool more = true;

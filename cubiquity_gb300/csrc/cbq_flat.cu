@@ -34,7 +34,7 @@ __device__ __forceinline__ void flat_body(const Ctx& c, uint64_t n, unsigned lon
 
     Lane L;
     L.mode = kLaneIdle;
-    L.pending = false;
+    L.held = 0u;
     bool more = PERSISTENT;  // warp-uniform: the queue may still hold rays
     if (!PERSISTENT) {
         const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;

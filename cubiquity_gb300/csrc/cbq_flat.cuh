@@ -47,7 +47,7 @@ struct Lane {
     float last_exit;
     uint32_t fetches, status, mode;
     bool fast;                   // no slab distance can be NaN or -0: min/max need no NaN ordering
-    bool pending;                // finished in this step batch, result held in node/last_exit/cid
+    uint32_t held;               // finished in this step batch: 0 no, 1 miss (status set), 2 hit at child `node`
     uint32_t loads;              // node loads made (fetches minus skipped empty children)
     uint32_t job;                // batch kernel: index of the lane's job
     uint64_t ray;                // ray index within its job
@@ -186,39 +186,49 @@ __device__ __forceinline__ void lane_finish(Lane& L, const Src& c, bool hit, flo
     L.mode = kLaneIdle;
 }
 
-// A finish inside the step loop.  The result is held in walk state that is
-// dead once the ray is done (node: hit | status << 8 | entry-plane bits << 16
-// | surface << 19; last_exit: distance; cid: material) and written by
-// flush_held after the step batch, by all the warp's lanes that finished in
-// it at once: finishes are spread over the steps, so writing each at once ran
-// the result code (position, normal, thirteen stores) at a few active lanes.
-__device__ __forceinline__ void lane_hold(Lane& L, bool hit, float dist, uint32_t material, uint32_t planes,
-                                          bool surface)
+// A finish inside the step loop.  The lane only records how it ended (a miss,
+// with its status; or a hit at child `node` of the current child position) and
+// flush_held completes the result after the step batch, for all the warp's
+// lanes that finished in it at once: finishes are spread over the steps, so
+// completing each at once ran the result code at a few active lanes.
+__device__ __forceinline__ void lane_hold_miss(Lane& L)
 {
-    L.node = (hit ? 1u : 0u) | (L.status << 8) | (planes << 16) | (surface ? (1u << 19) : 0u);
-    L.last_exit = dist;
-    L.cid = material;
-    L.pending = true;
+    L.held = 1u;
     L.mode = kLaneIdle;
 }
 
-// Writes a held result: the normal is the reference's
-// vec3(equal(tChildEntry, childT0)) * -rayDirSign (raytracing.cpp:314-315),
-// from the held plane bits.
+// Completes a held result with the reference's operations: the entry distance
+// max3(childT0) (raytracing.cpp:270-271), the material (findNearestMaterial,
+// :310) and the normal vec3(equal(tChildEntry, childT0)) * -rayDirSign
+// (:317-318).  For rays on the fast min/max path max3 gives the same bits.
 template <typename Src>
 __device__ __forceinline__ void flush_held(Lane& L, const Src& c)
 {
-    if (!L.pending) return;
-    L.pending = false;
-    const uint32_t w = L.node;
-    float nx = 0.0f, ny = 0.0f, nz = 0.0f;
-    if (w & (1u << 19)) {
-        nx = __fmul_rn((w & (1u << 16)) ? 1.0f : 0.0f, (L.sign & 1u) ? 1.0f : -1.0f);
-        ny = __fmul_rn((w & (1u << 17)) ? 1.0f : 0.0f, (L.sign & 2u) ? 1.0f : -1.0f);
-        nz = __fmul_rn((w & (1u << 18)) ? 1.0f : 0.0f, (L.sign & 4u) ? 1.0f : -1.0f);
+    if (!L.held) return;
+    const uint32_t kind = L.held;
+    L.held = 0u;
+    if (kind == 1u) {
+        lane_finish(L, c, false, 0.0f, 0u, 0.0f, 0.0f, 0.0f);
+        return;
     }
-    L.status = (w >> 8) & 0xffu;
-    lane_finish(L, c, w & 1u, L.last_exit, L.cid, nx, ny, nz);
+    constexpr bool INT = Src::kIntPos;
+    const float c0x = ((INT ? (float)L.px : L.fx) - L.rox) * L.ix;
+    const float c0y = ((INT ? (float)L.py : L.fy) - L.roy) * L.iy;
+    const float c0z = ((INT ? (float)L.pz : L.fz) - L.roz) * L.iz;
+    const float tce = max3_ref(c0x, c0y, c0z);
+    uint32_t material = 0u;
+    float nx = 0.0f, ny = 0.0f, nz = 0.0f;
+    if (c.query(L).compute_surface) {
+        material = nearest_material<Src::kCompact, INT>(c.nodes(L), L.node, L.sign, L.fetches, L.status, L.loads);
+        if (L.status != kRayOk) {
+            lane_finish(L, c, false, 0.0f, 0u, 0.0f, 0.0f, 0.0f);
+            return;
+        }
+        nx = __fmul_rn(tce == c0x ? 1.0f : 0.0f, (L.sign & 1u) ? 1.0f : -1.0f);
+        ny = __fmul_rn(tce == c0y ? 1.0f : 0.0f, (L.sign & 2u) ? 1.0f : -1.0f);
+        nz = __fmul_rn(tce == c0z ? 1.0f : 0.0f, (L.sign & 4u) ? 1.0f : -1.0f);
+    }
+    lane_finish(L, c, true, tce, material, nx, ny, nz);
 }
 
 // One octant transition (raytracing.cpp:469-475).
@@ -317,11 +327,11 @@ __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
     const uint32_t child = child_of<Src::kCompact, INT>(c.nodes(L), L.node, L.cid ^ L.sign, L.loads);
     L.fetches++;
     if (child > 0u) {
-        const float c0x = ((INT ? (float)L.px : L.fx) - L.rox) * L.ix;
-        const float c0y = ((INT ? (float)L.py : L.fy) - L.roy) * L.iy;
-        const float c0z = ((INT ? (float)L.pz : L.fz) - L.roz) * L.iz;
-        const float tce = slab_max3<FAST>(c0x, c0y, c0z);
         if (child >= kMaterialCount && large_footprint(L.cns, tcx, c.query(L).max_footprint)) {
+            const float c0x = ((INT ? (float)L.px : L.fx) - L.rox) * L.ix;
+            const float c0y = ((INT ? (float)L.py : L.fy) - L.roy) * L.iy;
+            const float c0z = ((INT ? (float)L.pz : L.fz) - L.roz) * L.iz;
+            const float tce = slab_max3<FAST>(c0x, c0y, c0z);
             if (tcx < L.last_exit) stack.put(L.h, L.node);
             L.last_exit = tcx;
             L.h--;
@@ -342,19 +352,10 @@ __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
                 L.fy = by ? mcy : L.fy;
                 L.fz = bz ? mcz : L.fz;
             }
-        } else {
-            uint32_t material = 0u, planes = 0u;
-            const bool surface = c.query(L).compute_surface;
-            if (surface) {
-                material = nearest_material<Src::kCompact, INT>(c.nodes(L), child, L.sign, L.fetches, L.status,
-                                                                L.loads);
-                if (L.status != kRayOk) {
-                    lane_hold(L, false, 0.0f, 0u, 0u, false);
-                    return;
-                }
-                planes = (tce == c0x ? 1u : 0u) | (tce == c0y ? 2u : 0u) | (tce == c0z ? 4u : 0u);
-            }
-            lane_hold(L, true, tce, material, planes, surface);
+        } else {  // a hit at this child: completed by flush_held
+            L.node = child;
+            L.held = 2u;
+            L.mode = kLaneIdle;
         }
         return;
     }
@@ -364,7 +365,7 @@ __device__ __forceinline__ void lane_walk(Lane& L, const Src& c, Stack& stack)
     // and that axis flips: only the reference's form can get stuck here.
     if (!FAST && !(ax || ay || az)) {
         L.status = kRayStuck;
-        lane_hold(L, false, 0.0f, 0u, 0u, false);
+        lane_hold_miss(L);
         return;
     }
     L.cid ^= flips;
@@ -444,7 +445,7 @@ __device__ __forceinline__ void lane_walk_steps(Lane& L, const Src& c, Stack& st
     while (L.fetches < end && L.mode == kLaneWalk) lane_walk<FAST>(L, c, stack);
     if (L.mode == kLaneWalk && L.fetches >= kMaxFetches) {
         L.status = kRayIterLimit;
-        lane_hold(L, false, 0.0f, 0u, 0u, false);
+        lane_hold_miss(L);
     }
 }
 
