@@ -77,6 +77,8 @@ def parse_args():
                         "from the checkout (else the oracle's C restatement), or the restatement always")
     p.add_argument("--no-extras", action="store_true",
                    help="terrain-4096: skip the batch-64 and serve-8 measurements added to the line")
+    p.add_argument("--no-image-order", dest="image_order", action="store_false",
+                   help="do not pass the camera batch's image width (rays then taken in the order given)")
     p.add_argument("--layout", choices=["reference", "compact"], default="reference",
                    help="device node store: the reference's array, or the compact store (occupied children only)")
     p.add_argument("--node-order", choices=["builder", "bfs"], default="builder",
@@ -110,6 +112,15 @@ def make_workload(name: str):
     nodes, root = W.TERRAIN_4096.build()
     o, d = W.TERRAIN_4096_CAMERA.rays()
     return nodes, root, [("primary", o, d)], "bounce"
+
+
+def image_widths(name: str) -> dict:
+    """Batches whose rays are a camera's pixels in row-major order, with the
+    image width (passed as the query's image_width: the kernel may take them
+    in image tiles; the bounce rays are not an image)."""
+    from cubiquity_gb300 import workloads as W
+    cam = W.SPHERES_256_CAMERA if name == "spheres-256" else W.TERRAIN_4096_CAMERA
+    return {"primary": cam.width}
 
 
 def bounce_batch(dag, o, d):
@@ -343,6 +354,7 @@ def run_gpu(args, world, rank, local):
     serve = serve_in_own_process(args, local) if extras else None
     torch.cuda.set_device(local)
     nodes, root, batches, bounce = make_workload(args.workload)
+    widths = image_widths(args.workload) if args.image_order else {}
     dag = cbq.Dag(nodes, root, LAYOUTS[args.layout])
     kernel_id = {"auto": cbq.KERNEL_AUTO, "flat": cbq.KERNEL_FLAT, "nested": cbq.KERNEL_NESTED}[args.kernel]
     dag.set_launch_config(kernel_id, args.block, args.chunk if not args.persistent else 0, 0)
@@ -367,7 +379,7 @@ def run_gpu(args, world, rank, local):
         from cubiquity_gb300 import autotune
         scratch = cbq.scratch_for(max(b[1].shape[0] for b in dev_batches))
         for label, to, td, out, _ in dev_batches:
-            tuned[label] = autotune.tune(dag, to, td, scratch, out, stream=stream)
+            tuned[label] = autotune.tune(dag, to, td, scratch, out, stream=stream, image_width=widths.get(label, 0))
         torch.cuda.synchronize()
 
     def launch(label, to, td, out):
@@ -375,11 +387,12 @@ def run_gpu(args, world, rank, local):
             c = tuned[label]
             dag.set_launch_config(c["kernel"], c["block"], c["chunk"], c["refill_min"], c["stack"], c["form"],
                                   c.get("steps", 1), c.get("registers", 0))
-            cbq.intersect_auto(dag, to, td, scratch, out=out, stream=stream)
+            cbq.intersect_auto(dag, to, td, scratch, out=out, stream=stream, image_width=widths.get(label, 0))
         elif args.persistent:
-            cbq.intersect_volume_persistent(dag, to, td, counter, chunk=args.chunk, out=out, stream=stream)
+            cbq.intersect_volume_persistent(dag, to, td, counter, chunk=args.chunk, out=out, stream=stream,
+                                            image_width=widths.get(label, 0))
         else:
-            cbq.intersect_volume(dag, to, td, out=out, stream=stream)
+            cbq.intersect_volume(dag, to, td, out=out, stream=stream, image_width=widths.get(label, 0))
 
     def step(events=None):
         for i, (label, to, td, out, _) in enumerate(dev_batches):
@@ -485,7 +498,7 @@ def run_gpu(args, world, rank, local):
 
     def e2e_call(item):
         label, po, pd, outs = item
-        cbq.intersect_volume_host(e2e_dags[label], po, pd, out=outs)
+        cbq.intersect_volume_host(e2e_dags[label], po, pd, out=outs, image_width=widths.get(label, 0))
 
     # The batches are independent streams of work, so a caller issues them from
     # one host thread per batch, and the calls of different threads overlap
@@ -547,6 +560,7 @@ def run_gpu(args, world, rank, local):
         "config": {"workload": args.workload, "rays_per_step": rays_per_step, "kernel": kernel_name,
                    "form": args.form, "launch_config": tuned if tuned else cfg,
                    "batches": {b[0]: int(b[1].shape[0]) for b in dev_batches},
+                   "image_width": widths,
                    "dag_nodes": int(dag.node_count), "dag_bytes": int(dag.bytes),
                    "layout": args.layout, "device_node_bytes": int(dag.device_bytes),
                    "l2": "inputs larger than L2 (rays + hits %.0f MB per step); DAG read through L2"

@@ -62,7 +62,7 @@ class _Hits(ctypes.Structure):
 
 class _Query(ctypes.Structure):
     _fields_ = [("compute_surface", ctypes.c_int32), ("max_footprint", ctypes.c_float),
-                ("flags", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("flags", ctypes.c_uint32), ("image_width", ctypes.c_uint32)]
 
 
 KERNEL_AUTO, KERNEL_NESTED, KERNEL_FLAT = 0, 1, 2
@@ -351,10 +351,11 @@ class Query:
     compute_surface_properties: bool = True
     max_footprint: float = MAX_FOOTPRINT_DISABLED
     use_tmax: bool = False
+    image_width: int = 0  # rays are the pixels of a row-major image this wide (see cbq_query)
 
     def c(self) -> _Query:
         return _Query(1 if self.compute_surface_properties else 0, float(self.max_footprint),
-                      QUERY_TMAX if self.use_tmax else 0, 0)
+                      QUERY_TMAX if self.use_tmax else 0, int(self.image_width))
 
 
 class Dag:
@@ -447,7 +448,7 @@ def _check_rays_tensor(t, n=None):
 
 def intersect_volume(dag: Dag, origin_tmax, direction, compute_surface_properties: bool = True,
                      max_footprint: float = MAX_FOOTPRINT_DISABLED, use_tmax: bool = False, out: dict | None = None,
-                     stream=None) -> dict:
+                     stream=None, image_width: int = 0) -> dict:
     """Batched intersectVolume (raytracing.cpp:397-478) on device tensors.
 
     origin_tmax, direction: float32 CUDA tensors (n, 4).  Returns a dict of
@@ -459,7 +460,7 @@ def intersect_volume(dag: Dag, origin_tmax, direction, compute_surface_propertie
     if out is None:
         out = alloc_hits(n, origin_tmax.device)
     rays = _Rays(origin_tmax.data_ptr(), direction.data_ptr())
-    q = Query(compute_surface_properties, max_footprint, use_tmax).c()
+    q = Query(compute_surface_properties, max_footprint, use_tmax, image_width).c()
     _check(_lib.cbq_intersect(dag.handle, ctypes.byref(rays), n, ctypes.byref(q), ctypes.byref(_hits_struct(out)),
                               _stream_ptr(stream)), "cbq_intersect")
     return out
@@ -467,7 +468,7 @@ def intersect_volume(dag: Dag, origin_tmax, direction, compute_surface_propertie
 
 def intersect_volume_persistent(dag: Dag, origin_tmax, direction, work_counter, compute_surface_properties=True,
                                 max_footprint=MAX_FOOTPRINT_DISABLED, use_tmax=False, chunk: int = 0,
-                                out: dict | None = None, stream=None) -> dict:
+                                out: dict | None = None, stream=None, image_width: int = 0) -> dict:
     """The persistent-warp form; ``work_counter`` is an int64 CUDA tensor (>= 1 element)."""
     _check_rays_tensor(origin_tmax)
     n = origin_tmax.shape[0]
@@ -475,7 +476,7 @@ def intersect_volume_persistent(dag: Dag, origin_tmax, direction, work_counter, 
     if out is None:
         out = alloc_hits(n, origin_tmax.device)
     rays = _Rays(origin_tmax.data_ptr(), direction.data_ptr())
-    q = Query(compute_surface_properties, max_footprint, use_tmax).c()
+    q = Query(compute_surface_properties, max_footprint, use_tmax, image_width).c()
     _check(_lib.cbq_intersect_persistent(dag.handle, ctypes.byref(rays), n, ctypes.byref(q),
                                          ctypes.byref(_hits_struct(out)), work_counter.data_ptr(), chunk,
                                          _stream_ptr(stream)), "cbq_intersect_persistent")
@@ -489,7 +490,8 @@ def scratch_for(n: int, device="cuda"):
 
 
 def intersect_auto(dag: Dag, origin_tmax, direction, scratch, compute_surface_properties=True,
-                   max_footprint=MAX_FOOTPRINT_DISABLED, use_tmax=False, out: dict | None = None, stream=None) -> dict:
+                   max_footprint=MAX_FOOTPRINT_DISABLED, use_tmax=False, out: dict | None = None, stream=None,
+                   image_width: int = 0) -> dict:
     """Traverses with the form and launch shape in the DAG's launch config
     (plain, persistent or octant-sorted persistent), e.g. as set by autotune()."""
     _check_rays_tensor(origin_tmax)
@@ -498,18 +500,19 @@ def intersect_auto(dag: Dag, origin_tmax, direction, scratch, compute_surface_pr
     if out is None:
         out = alloc_hits(n, origin_tmax.device)
     rays = _Rays(origin_tmax.data_ptr(), direction.data_ptr())
-    q = Query(compute_surface_properties, max_footprint, use_tmax).c()
+    q = Query(compute_surface_properties, max_footprint, use_tmax, image_width).c()
     _check(_lib.cbq_intersect_auto(dag.handle, ctypes.byref(rays), n, ctypes.byref(q), ctypes.byref(_hits_struct(out)),
                                    scratch.data_ptr(), scratch.numel(), _stream_ptr(stream)), "cbq_intersect_auto")
     return out
 
 
 def autotune_launch(dag: Dag, origin_tmax, direction, scratch, out: dict, compute_surface_properties=True,
-                    max_footprint=MAX_FOOTPRINT_DISABLED, use_tmax=False, repetitions: int = 3, stream=None):
+                    max_footprint=MAX_FOOTPRINT_DISABLED, use_tmax=False, repetitions: int = 3, stream=None,
+                    image_width: int = 0):
     """Runs the native autotuner on these rays; returns (config dict, ms per launch)."""
     n = origin_tmax.shape[0]
     rays = _Rays(origin_tmax.data_ptr(), direction.data_ptr())
-    q = Query(compute_surface_properties, max_footprint, use_tmax).c()
+    q = Query(compute_surface_properties, max_footprint, use_tmax, image_width).c()
     best = LaunchConfig()
     ms = ctypes.c_float()
     _check(_lib.cbq_autotune(dag.handle, ctypes.byref(rays), n, ctypes.byref(q), ctypes.byref(_hits_struct(out)),
@@ -540,7 +543,7 @@ def alloc_host_hits(n: int) -> dict:
 
 def intersect_volume_host(dag: Dag, origin_tmax: np.ndarray, direction: np.ndarray,
                           compute_surface_properties: bool = True, max_footprint: float = MAX_FOOTPRINT_DISABLED,
-                          use_tmax: bool = False, out: dict | None = None) -> dict:
+                          use_tmax: bool = False, out: dict | None = None, image_width: int = 0) -> dict:
     """Host-buffer form (cbq_intersect_host): copies in, traverses, copies out."""
     o = np.ascontiguousarray(origin_tmax, dtype=np.float32).reshape(-1, 4)
     d = np.ascontiguousarray(direction, dtype=np.float32).reshape(-1, 4)
@@ -550,7 +553,7 @@ def intersect_volume_host(dag: Dag, origin_tmax: np.ndarray, direction: np.ndarr
     if out is None:
         out = alloc_host_hits(n)
     hits = _Hits(*[_np_ptr(out.get(k)) for k in HIT_FIELDS])
-    q = Query(compute_surface_properties, max_footprint, use_tmax).c()
+    q = Query(compute_surface_properties, max_footprint, use_tmax, image_width).c()
     _check(_lib.cbq_intersect_host(dag.handle, _np_ptr(o), _np_ptr(d), n, ctypes.byref(q), ctypes.byref(hits)),
            "cbq_intersect_host")
     return out
@@ -606,7 +609,7 @@ _sig("cbq_server_replay", [_P, _P, _P, _U64, _U32, _P, ctypes.POINTER(_ReplayRes
 # loop per request (pointers as integers; 0 = NULL).
 REQUEST_DTYPE = np.dtype([("dag", np.uint64), ("origin_tmax", np.uint64), ("direction", np.uint64),
                           ("ray_count", np.uint64), ("compute_surface", np.int32), ("max_footprint", np.float32),
-                          ("flags", np.uint32), ("reserved", np.uint32)] +
+                          ("flags", np.uint32), ("image_width", np.uint32)] +
                          [(k, np.uint64) for k in HIT_FIELDS])
 assert REQUEST_DTYPE.itemsize == ctypes.sizeof(_Request)
 

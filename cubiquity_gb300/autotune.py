@@ -61,9 +61,11 @@ def _store(cache: dict) -> None:
 
 def tune(dag: cbq.Dag, origin_tmax, direction, scratch, out: dict, compute_surface_properties=True,
          max_footprint=cbq.MAX_FOOTPRINT_DISABLED, use_tmax=False, repetitions: int = 3, use_cache: bool = True,
-         stream=None) -> dict:
-    """Applies (and returns) the best launch config for this DAG and ray mix."""
-    key = cache_key(dag, direction)
+         stream=None, image_width: int = 0) -> dict:
+    """Applies (and returns) the best launch config for this DAG and ray mix
+    (rays taken in image tiles when image_width is given: tuned, and cached,
+    apart from rays taken in order)."""
+    key = cache_key(dag, direction) + ("|image" if image_width else "")
     cache = _load() if use_cache else {}
     if key in cache:
         cfg = dict(cache[key]["config"])
@@ -73,7 +75,7 @@ def tune(dag: cbq.Dag, origin_tmax, direction, scratch, out: dict, compute_surfa
                               cfg["steps"], cfg["registers"])
         return dict(cfg, cached=True, key=key)
     cfg, ms = cbq.autotune_launch(dag, origin_tmax, direction, scratch, out, compute_surface_properties,
-                                  max_footprint, use_tmax, repetitions, stream)
+                                  max_footprint, use_tmax, repetitions, stream, image_width)
     if use_cache:
         cache = _load()
         cache[key] = {"config": cfg, "ms": ms, "rays": int(origin_tmax.shape[0])}

@@ -64,6 +64,7 @@ dev::QueryParams make_query(const cbq_query* q)
     p.compute_surface = q ? q->compute_surface : 1;
     p.max_footprint = q ? q->max_footprint : CBQ_MAX_FOOTPRINT_DISABLED;
     p.flags = q ? q->flags : 0u;
+    p.image_width = q ? q->image_width : 0u;  // checked against each launch's ray count by launch_flat
     return p;
 }
 

@@ -38,7 +38,7 @@ __device__ __forceinline__ void flat_body(const Ctx& c, uint64_t n, unsigned lon
     bool more = PERSISTENT;  // warp-uniform: the queue may still hold rays
     if (!PERSISTENT) {
         const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-        if (i < n) lane_begin(L, c, SORTED ? (uint64_t)__ldg(perm + i) : i);
+        if (i < n) lane_begin(L, c, SORTED ? (uint64_t)__ldg(perm + i) : c.ray_slot(i));
     }
     for (;;) {
         if (PERSISTENT && more) {
@@ -51,7 +51,7 @@ __device__ __forceinline__ void flat_body(const Ctx& c, uint64_t n, unsigned lon
                 base = __shfl_sync(kFull, base, leader);
                 if (L.mode == kLaneIdle) {
                     const uint64_t i = base + __popc(idle & below);
-                    if (i < n) lane_begin(L, c, SORTED ? (uint64_t)__ldg(perm + i) : i);
+                    if (i < n) lane_begin(L, c, SORTED ? (uint64_t)__ldg(perm + i) : c.ray_slot(i));
                 }
                 if (base + cnt >= n) more = false;
             }
@@ -268,10 +268,16 @@ Ctx make_ctx(const dev::DagParams& dp, const dev::QueryParams& q, const dev::Hit
     return c;
 }
 
-cbq_status launch_flat(const cbq_dag* dag, const dev::DagParams& dp, const dev::QueryParams& q,
+cbq_status launch_flat(const cbq_dag* dag, const dev::DagParams& dp, const dev::QueryParams& query,
                        const dev::HitsOut& out, const float4* orig, const float4* dir, uint64_t n,
                        uint32_t* fetch_out, const FlatLaunch& fl, cudaStream_t stream)
 {
+    // The image order applies where it is a bijection of this launch's rays:
+    // whole 8-row bands of a width that is a multiple of 4, 32-bit indices.
+    dev::QueryParams q = query;
+    const uint64_t band = 8ull * q.image_width;
+    if (q.image_width && ((q.image_width & 3u) || n >= (1ull << 32) || n % band != 0 || fl.perm))
+        q.image_width = 0u;
     if (fl.persistent && !fl.counter) return CBQ_ERR_INVALID_ARGUMENT;
     if (fl.perm && n >= 0xffffffffull) return CBQ_ERR_INVALID_ARGUMENT;
     const int rows = std::max(1, (int)dag->max_height);

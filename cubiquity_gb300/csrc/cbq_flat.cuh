@@ -78,6 +78,19 @@ struct FlatCtxT {
 
     __device__ __forceinline__ const QueryParams& query(const Lane&) const { return q; }
     __device__ __forceinline__ const uint32_t* nodes(const Lane&) const { return dag.nodes; }
+    // Ray of work item g: g itself, or with an image width (q.image_width, a
+    // multiple of 4 dividing the launch into whole 8-row bands) the pixel of
+    // tile g / 32 (tiles of 4 x 8 pixels, a band's tiles left to right) at
+    // place g % 32 (row-major in the tile): a bijection of [0, n).
+    __device__ __forceinline__ uint64_t ray_slot(uint64_t g) const
+    {
+        const uint32_t w = q.image_width;
+        if (w == 0u) return g;
+        const uint32_t t = (uint32_t)(g >> 5), k = (uint32_t)g & 31u;
+        const uint32_t per_band = w >> 2;
+        const uint32_t band = t / per_band, col = t - band * per_band;
+        return (uint64_t)(band * 8u + (k >> 2)) * w + col * 4u + (k & 3u);
+    }
     __device__ __forceinline__ const SubDag& subdag(const Lane&, uint32_t k) const { return dag.sd[k]; }
     // Rays are read once: streaming loads (evict-first) leave L2 to the node store.
     __device__ __forceinline__ float4 ray_origin(const Lane&, uint64_t i) const { return __ldcs(orig + i); }

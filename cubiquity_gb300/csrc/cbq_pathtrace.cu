@@ -320,6 +320,9 @@ extern "C" cbq_status cbq_pathtrace(const cbq_dag* dag, const cbq_pt_config* cfg
 
     const cbq_query qext{1, cfg->max_footprint, 0u, 0u};
     const cbq_query qsh{0, cfg->max_footprint, 0u, 0u};
+    // The camera wave's paths are the pass's samples' images stacked in row-major
+    // order: the traversal may deal them to warps in image tiles.
+    const cbq_query qcam{1, cfg->max_footprint, 0u, (uint32_t)cfg->width};
     for (int sample = 0; sample < cfg->samples_per_pixel && st == CBQ_OK; sample += (int)per_pass) {
         const uint32_t samples = (uint32_t)std::min<uint64_t>(per_pass, (uint64_t)(cfg->samples_per_pixel - sample));
         Frame fr;
@@ -346,13 +349,14 @@ extern "C" cbq_status cbq_pathtrace(const cbq_dag* dag, const cbq_pt_config* cfg
             Ext& N = e[cur ^ 1];
             cbq_rays rays{(const float*)E.o, (const float*)E.d};
             cbq_hits hits{E.hit, nullptr, E.material, E.position, E.normal, nullptr, nullptr};
-            cbq_status ts = cbq_intersect_persistent(dag, &rays, n, &qext, &hits, work, 0u, (cbq_stream_t)s);
+            const cbq_query* qe = depth == 0 ? &qcam : &qext;
+            cbq_status ts = cbq_intersect_persistent(dag, &rays, n, qe, &hits, work, 0u, (cbq_stream_t)s);
             if (ts != CBQ_OK) { fail(ts); break; }
             ext_rays += n;
             launches++;
             if (on_wave) {
                 if (cudaStreamSynchronize(s) != cudaSuccess) { fail(CBQ_ERR_CUDA); break; }
-                on_wave(user, 0, depth, sample, (const float*)E.o, (const float*)E.d, n, &hits, &qext);
+                on_wave(user, 0, depth, sample, (const float*)E.o, (const float*)E.d, n, &hits, qe);
             }
             if (cudaMemsetAsync(counters, 0, 8 * sizeof(uint32_t), s) != cudaSuccess) { fail(CBQ_ERR_CUDA); break; }
             const int last = depth == cfg->bounces;

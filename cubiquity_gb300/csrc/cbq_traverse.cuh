@@ -41,6 +41,7 @@ struct QueryParams {
     int32_t compute_surface;
     float max_footprint;
     uint32_t flags;
+    uint32_t image_width;  // flat kernels: rays dealt in 4x8 tiles of an image this wide (0: in order)
 };
 
 struct HitsOut {

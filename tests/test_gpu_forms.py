@@ -109,6 +109,43 @@ def test_l2_probes():
         cbq.measure_l2(32 << 20, 0)
 
 
+@pytest.mark.parametrize("form", [cbq.FORM_PLAIN, cbq.FORM_PERSISTENT, cbq.FORM_SORTED])
+@pytest.mark.parametrize("width", [384, 96, 12, 4, 12288, 383, 392])
+def test_image_order_gives_the_same_bits(scene, form, width):
+    """Rays dealt to warps in 4x8 tiles of an image (query image_width): the same
+    bits as rays in order, every ray written once (outputs start as a sentinel).
+    384 is the camera's own width; 96, 12, 4 and 12288 (one band) also tile the
+    98,304 rays; 383 (not a multiple of 4) and 392 (not whole 8-row bands) are
+    ignored by the launch; the sorted form keeps its octant order."""
+    dag, rays = scene
+    dag.set_launch_config(cbq.KERNEL_FLAT, 128, 0, 8, cbq.STACK_SHARED, form, 8)
+    try:
+        for label in ("primary", "bounce"):
+            o, d = rays[label]
+            scratch = cbq.scratch_for(o.shape[0])
+            want = cbq.intersect_auto(dag, o, d, scratch)
+            out = cbq.alloc_hits(o.shape[0])
+            for v in out.values():
+                v.view(torch.uint8).fill_(0xA5)
+            got = cbq.intersect_auto(dag, o, d, scratch, out=out, image_width=width)
+            _same(got, want)
+            got2 = cbq.intersect_volume(dag, o, d, image_width=width)
+            _same(got2, want)
+    finally:
+        dag.set_launch_config()
+
+
+def test_image_order_through_the_host_entry_point(scene):
+    """cbq_intersect_host with an image width: its chunks take the image order
+    where they are whole bands; the bits equal the device call's."""
+    dag, rays = scene
+    o, d = rays["primary"]
+    want = cbq.intersect_volume(dag, o, d)
+    got = cbq.intersect_volume_host(dag, o.cpu().numpy(), d.cpu().numpy(), image_width=384)
+    for k in FIELDS:
+        assert oracle.same_bits_nan_equal(got[k], want[k].cpu().numpy()), k
+
+
 def test_drop_in_on_concurrent_streams_and_in_a_graph(scene):
     """cbq_intersect's persistent form keeps one work counter per stream: launches
     on several streams at once, and one captured into a CUDA graph (the plain
