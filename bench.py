@@ -71,6 +71,9 @@ def parse_args():
     p.add_argument("--block", type=int, default=0)
     p.add_argument("--chunk", type=int, default=0, help="persistent: refill threshold (flat) / grab size (nested)")
     p.add_argument("--e2e-steps", type=int, default=20)
+    p.add_argument("--e2e-threads", type=int, default=0,
+                   help="host threads issuing the e2e calls (0: one per batch); threads x calls per thread = "
+                        "batches x e2e steps")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-impl", choices=["auto", "port"], default="auto",
                    help="CPU ray cast timed by --impl reference: the reference's own library where it was built "
@@ -484,6 +487,13 @@ def run_gpu(args, world, rank, local):
                 "position": torch.empty((n, 3), dtype=torch.float32).pin_memory(),
                 "normal": torch.empty((n, 3), dtype=torch.float32).pin_memory()}
         host.append((label, po.numpy(), pd.numpy(), {k: v.numpy() for k, v in outs.items()}))
+    # Calls in flight at once: one host thread per batch by default; each thread
+    # has its own output buffers.
+    e2e_threads = args.e2e_threads or len(host)
+    thread_outs = [[h[3] for h in host]]
+    for _ in range(1, e2e_threads):
+        thread_outs.append([{k: torch.empty(v.shape, dtype=torch.from_numpy(v).dtype).pin_memory().numpy()
+                             for k, v in h[3].items()} for h in host])
 
     # One DAG handle per batch, so each keeps the launch shape tuned for it (a
     # handle's launch configuration is shared by its callers).
@@ -496,27 +506,34 @@ def run_gpu(args, world, rank, local):
                                 c.get("steps", 1), c.get("registers", 0))
         e2e_dags[label] = g
 
-    def e2e_call(item):
-        label, po, pd, outs = item
-        cbq.intersect_volume_host(e2e_dags[label], po, pd, out=outs, image_width=widths.get(label, 0))
+    def e2e_call(item, outs=None):
+        label, po, pd, own = item
+        cbq.intersect_volume_host(e2e_dags[label], po, pd, out=own if outs is None else outs,
+                                  image_width=widths.get(label, 0))
 
     # The batches are independent streams of work, so a caller issues them from
-    # one host thread per batch, and the calls of different threads overlap
-    # their copies and traversals (the host entry point is thread-safe).  The
-    # threads alternate the batches (thread t's k-th call is batch (t + k) mod
-    # the number of batches), so each makes one call of every batch per round of
-    # calls and no thread is left running alone at the end; over all threads
-    # each batch is called e2e_steps times.  The clock runs from the start until
-    # every thread has made its calls, i.e. every step's rays were copied in and
-    # its hits copied out.  The single-thread figure (the batches' calls one
-    # after the other) is kept beside it.
+    # several host threads (one per batch by default, --e2e-threads), and the
+    # calls of different threads overlap their copies and traversals (the host
+    # entry point is thread-safe).  The threads alternate the batches (thread
+    # t's k-th call is batch (t + k) mod the number of batches), so no thread is
+    # left running alone at the end; over all threads each batch is called
+    # e2e_steps times (threads x calls per thread = batches x e2e_steps).  The
+    # clock runs from the start until every thread has made its calls, i.e.
+    # every step's rays were copied in and its hits copied out.  The
+    # single-thread figure (the batches' calls one after the other) is kept
+    # beside it.
+    if (args.e2e_steps * len(host)) % e2e_threads:
+        raise SystemExit("--e2e-threads must divide the e2e calls (batches x --e2e-steps)")
+    calls_per_thread = args.e2e_steps * len(host) // e2e_threads
+
     def e2e_timed(threaded: bool) -> float:
         errors = []
 
         def worker(t):
             try:
-                for k in range(args.e2e_steps):
-                    e2e_call(host[(t + k) % len(host)])
+                for k in range(calls_per_thread):
+                    b = (t + k) % len(host)
+                    e2e_call(host[b], thread_outs[t][b])
             except Exception as e:  # noqa: BLE001  (re-raised below: a failed call voids the figure)
                 errors.append(e)
         for h in host:  # warm-up: staging sets allocated
@@ -524,7 +541,7 @@ def run_gpu(args, world, rank, local):
         barrier(world)
         t = time.perf_counter()
         if threaded:
-            th = [threading.Thread(target=worker, args=(t,)) for t in range(len(host))]
+            th = [threading.Thread(target=worker, args=(t,)) for t in range(e2e_threads)]
             for x in th:
                 x.start()
             for x in th:
@@ -535,9 +552,11 @@ def run_gpu(args, world, rank, local):
             for _ in range(args.e2e_steps):
                 for h in host:
                     e2e_call(h)
-        return rays_per_step * args.e2e_steps * world / max_over_ranks(world, time.perf_counter() - t) / 1e6
+        rays = (sum(host[(t + k) % len(host)][1].shape[0] for t in range(e2e_threads) for k in range(calls_per_thread))
+                if threaded else rays_per_step * args.e2e_steps)
+        return rays * world / max_over_ranks(world, time.perf_counter() - t) / 1e6
 
-    e2e_value = e2e_timed(len(host) > 1)
+    e2e_value = e2e_timed(e2e_threads > 1)
     e2e_one_thread = e2e_timed(False)
     for g in e2e_dags.values():
         g.destroy()
@@ -574,8 +593,8 @@ def run_gpu(args, world, rank, local):
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": rays_per_step * RAY_BYTES,
                 "d2h_bytes_per_step": rays_per_step * REF_HIT_BYTES,
                 "api": "cbq_intersect_host (pinned host buffers, copies pipelined with the traversal inside), " +
-                       ("one call per batch and step, from %d host threads that alternate the batches" % len(host)
-                        if len(host) > 1 else "one call per step"),
+                       ("one call per batch and step, from %d host threads that alternate the batches" % e2e_threads
+                        if e2e_threads > 1 else "one call per step"),
                 "fields": "hit, distance, material, position, normal (the reference's RayVolumeIntersection)",
                 "steps": args.e2e_steps, "one_thread_value": e2e_one_thread},
         "gpu_launches": launches,
