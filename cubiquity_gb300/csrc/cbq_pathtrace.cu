@@ -124,26 +124,30 @@ __device__ __forceinline__ void add_pixel(float* image, uint32_t pixel, float r,
     atomicAdd(image + 3 * (size_t)pixel + 2, b);
 }
 
-// Appends one element to a compacted array with one atomic per warp.
-__device__ __forceinline__ uint32_t append_slot(uint32_t* counter, bool want)
+// Reserves the warp's slots in both compacted arrays with one 64-bit atomic
+// (all 32 lanes call it): two shadow rays per hit in the low word of `counts`
+// (the shadow count), one bounce ray per continuing path in the high word (the
+// bounce count).  A lane's shadow rays are slots s0 and s0 + 1.  One atomic
+// round trip per warp instead of three in a row: the kernel waits on memory.
+__device__ __forceinline__ void reserve_slots(unsigned long long* counts, bool hit, bool cont, uint32_t& s0,
+                                              uint32_t& b)
 {
-    const unsigned mask = __ballot_sync(0xffffffffu, want);
-    if (!want) return 0;
-    const int leader = __ffs(mask) - 1;
-    const unsigned lane = threadIdx.x & 31u;
-    uint32_t base = 0;
-    if ((int)lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
-    base = __shfl_sync(mask, base, leader);
-    return base + __popc(mask & ((1u << lane) - 1u));
+    const unsigned hm = __ballot_sync(0xffffffffu, hit), cm = __ballot_sync(0xffffffffu, cont);
+    const unsigned lane = threadIdx.x & 31u, below = (1u << lane) - 1u;
+    unsigned long long base = 0;
+    if (lane == 0 && (hm | cm))
+        base = atomicAdd(counts, 2ull * (unsigned)__popc(hm) | ((unsigned long long)(unsigned)__popc(cm) << 32));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    s0 = (uint32_t)base + 2u * (uint32_t)__popc(hm & below);
+    b = (uint32_t)(base >> 32) + (uint32_t)__popc(cm & below);
 }
 
 __global__ void cbq_k_pt_shade(const Shading* __restrict__ sh, uint32_t n, uint32_t depth, uint64_t seed, int last, const PathState* __restrict__ st,
                                const uint8_t* __restrict__ hit, const uint32_t* __restrict__ material,
                                const float* __restrict__ position, const float* __restrict__ normal,
                                float* __restrict__ image, float4* __restrict__ so, float4* __restrict__ sd,
-                               float4* __restrict__ sw, uint32_t* __restrict__ shadow_count,
-                               float4* __restrict__ no, float4* __restrict__ nd, PathState* __restrict__ nst,
-                               uint32_t* __restrict__ next_count)
+                               float4* __restrict__ sw, unsigned long long* __restrict__ counts,
+                               float4* __restrict__ no, float4* __restrict__ nd, PathState* __restrict__ nst)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = i < n;
@@ -167,9 +171,11 @@ __global__ void cbq_k_pt_shade(const Shading* __restrict__ sh, uint32_t n, uint3
         tb = p.tb * sh->albedo[m][2];
         key = rng_key(seed, p.pixel, p.sample, depth + 1, 0);
     }
-    // Two shadow rays per hit: sun and sky.
-    const uint32_t s0 = append_slot(shadow_count, h);
-    const uint32_t s1 = append_slot(shadow_count, h);
+    // Two shadow rays per hit (sun and sky) and a bounce ray per continuing path.
+    const bool cont = h && !last;
+    uint32_t s0 = 0, b = 0;
+    reserve_slots(counts, h, cont, s0, b);
+    const uint32_t s1 = s0 + 1u;
     if (h) {
         const float3 off = make_float3(nrm.x * 0.001f, nrm.y * 0.001f, nrm.z * 0.001f);
         const float3 org = make_float3(pos.x + off.x, pos.y + off.y, pos.z + off.z);
@@ -186,8 +192,6 @@ __global__ void cbq_k_pt_shade(const Shading* __restrict__ sh, uint32_t n, uint3
                              __uint_as_float(p.pixel));
     }
     // The bounce ray.
-    const bool cont = h && !last;
-    const uint32_t b = append_slot(next_count, cont);
     if (cont) {
         const float3 q = in_unit_sphere(mix64(key ^ 2u));
         const float3 dir = normalize3(make_float3(nrm.x + q.x, nrm.y + q.y, nrm.z + q.z));
@@ -281,7 +285,7 @@ extern "C" cbq_status cbq_pathtrace(const cbq_dag* dag, const cbq_pt_config* cfg
     }
     char* p = base;
     Shading* d_sh = carve<Shading>(p, 1);
-    uint32_t* counters = carve<uint32_t>(p, 8);           // [0] shadow count, [1] next count
+    uint32_t* counters = carve<uint32_t>(p, 8);           // [0] shadow count, [1] next count (one 64-bit word)
     uint64_t* work = carve<uint64_t>(p, 4);
     struct Ext {
         float4 *o, *d;
@@ -362,7 +366,7 @@ extern "C" cbq_status cbq_pathtrace(const cbq_dag* dag, const cbq_pt_config* cfg
             const int last = depth == cfg->bounces;
             cbq_k_pt_shade<<<(n + 255) / 256, 256, 0, s>>>(d_sh, n, (uint32_t)depth, cfg->seed, last,
                                                           E.st, E.hit, E.material, E.position, E.normal, device_image,
-                                                          so, sd, sw, counters, N.o, N.d, N.st, counters + 1);
+                                                          so, sd, sw, (unsigned long long*)counters, N.o, N.d, N.st);
             launches++;
             uint32_t h_counts[2] = {0, 0};
             if (cudaMemcpyAsync(h_counts, counters, sizeof(h_counts), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
