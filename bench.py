@@ -349,7 +349,7 @@ def run_gpu(args, world, rank, local):
     import torch
     import cubiquity_gb300 as cbq
 
-    # BASELINE's other two measurements ride on the default line (single-GPU
+    # The benchmark's other two measurements ride on the default line (single-GPU
     # runs): the serving latency (serve-8) first, by a child process, before
     # this process creates its CUDA context; the batched form (batch-64) after
     # the terrain.
@@ -913,7 +913,7 @@ def measure_serve(args, world, local, half_runs: int = 3, half_seconds: float = 
     request rate is found closed loop (every arrival at time 0, 64 requests
     outstanding), then an open-loop Poisson stream at half of it gives p50/p99
     latency (submit -> hits in host memory, timed by the server) and Mrays/s,
-    with the driver's lateness (actual submit time minus scheduled arrival)
+    with the trace driver's lateness (actual submit time minus scheduled arrival)
     beside them.  Returns (summary, details)."""
     import torch
     import cubiquity_gb300 as cbq

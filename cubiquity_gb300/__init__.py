@@ -668,7 +668,7 @@ class Server:
         """Open-loop replay of a request trace from native threads
         (cbq_server_replay): requests[k] (a REQUEST_DTYPE record whose buffers
         the caller keeps alive) is submitted arrival_s[k] seconds after the
-        start.  Returns the driver's result with per-request lateness (us)."""
+        start.  Returns the trace driver's result with per-request lateness (us)."""
         req = np.ascontiguousarray(requests, dtype=REQUEST_DTYPE)
         arr = np.ascontiguousarray(arrival_s, dtype=np.float64)
         if req.shape != arr.shape:
