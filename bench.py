@@ -11,6 +11,10 @@ Inputs are resident in HBM before timing; the ray and hit arrays (654 MB per
 step) exceed the 129 MB L2, so each step streams them; the 115 MB DAG is the
 traversal's working set and stays in L2.
 
+The camera batch passes its image width (the query's image_width), so the
+kernel takes its rays in 4x8 pixel tiles (same results; --no-image-order passes
+none); the bounce batch is not an image and goes in order.
+
 `value` is device throughput (CUDA events on the launching stream); `e2e` is the
 same workload through the host-buffer C ABI (cbq_intersect_host) with pinned
 host rays in and hits out, copies inside the timed region.  `roofline` is that
