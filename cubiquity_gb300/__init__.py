@@ -452,7 +452,9 @@ def intersect_volume(dag: Dag, origin_tmax, direction, compute_surface_propertie
     """Batched intersectVolume (raytracing.cpp:397-478) on device tensors.
 
     origin_tmax, direction: float32 CUDA tensors (n, 4).  Returns a dict of
-    device tensors (see HIT_FIELDS); pass ``out`` to reuse buffers.
+    device tensors (see HIT_FIELDS); pass ``out`` to reuse buffers.  When the
+    rays are the pixels of a row-major image, ``image_width`` lets the kernel
+    take them in 4x8 pixel tiles (same results; see cbq_query.image_width).
     """
     _check_rays_tensor(origin_tmax)
     n = origin_tmax.shape[0]
